@@ -1,0 +1,341 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 VBD step on the large spring cloth (263,169 vertices).
+
+One step = one spg::solver::VBD::step() equivalent on the 513x513 jittered spring cloth
+(787,456 springs k = 1e4, 785,408 bending stencils k = 1e-4, row 0 anchored), 20 VBD
+iterations per step at dt = 1/120 s, computed in FP32 on the GPU. Metric: vertex-solves/s =
+vertices x iterations x steps / device time. Inputs are resident in HBM when the timed region
+starts; L2 is flushed (256 MiB write) between timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU restatement of the reference VBD (the oracle, reference-literal
+full-element AD per incidence, OpenMP on all host cores) on bounded samples of the same
+workload: the reference itself does not build here (its Eigen and TinyAD submodules are empty).
+Multi-GPU runs are independent replicas (a single VBD mesh does not shard); value is the
+aggregate over ranks with the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "VBD vertex-solves/s on 263k-vert cloth; time-to-residual 1e-5, warm vs plain"
+UNIT = "vertex-solves/s"
+ROWS = 513
+ITERATIONS = 20
+DT = 1.0 / 120.0
+GRAVITY = (0.0, 0.0, -9.81)
+WORKLOAD = ("spring cloth 513x513 over 2 m (263169 verts, 787456 springs k=1e4, 785408 bending k=1e-4, "
+            "513 anchors), VBD 20 iterations/step, dt=1/120 s")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 0, 1
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return dist, rank, local, ws
+
+
+def _barrier(dist, local):
+    if dist is None:
+        return
+    import torch
+    torch.cuda.synchronize(local)
+    dist.barrier()
+
+
+def _max_over_ranks(dist, local, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(dist, local, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms while active."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes_per_iteration(obj) -> int:
+    """Compulsory FP32 bytes of one VBD iteration: per vertex 48 B (x read, x write, y and
+    mass), a 4 B incidence offset, 4 B per incidence, and every element record once (spring
+    16 B, bending 24 B, StVK 40 B, SNH 64 B, anchor 20 B)."""
+    from spg_gb300 import native as N
+    rec = {N.SPRING: 16, N.BENDING: 24, N.STVK: 40, N.SNH: 64, N.ANCHOR: 20}
+    nv = obj.nv
+    n_inc = sum(e.stencils.size for e in obj.energies)
+    return 48 * nv + 4 * (nv + 1) + 4 * n_inc + sum(rec[e.type] * e.n for e in obj.energies)
+
+
+def _measured_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic_per_iteration():
+    """DRAM bytes per colour sweep from the committed ncu summary, when present."""
+    p = os.path.join(ROOT, "profiles", "vbd_color_kernel_spring_cloth_513.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["dram_bytes_per_sweep"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_baseline(target_s: float = 12.0) -> dict:
+    """The oracle (CPU restatement of the reference VBD, reference-literal full-element AD per
+    incidence, OpenMP over each colour group) on whole colour sweeps of the same cloth, until
+    about target_s seconds of sweeping have run."""
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    w = 2.0
+    obj = O.build_spring_cloth(0.1 * w * w, w, w, ROWS, ROWS, 1e4, 1e-4, 1e5, 0.1, 12345)
+    s = O.Vbd(obj, DT, 1, ITERATIONS, GRAVITY, O.FULL_AD)
+    s.begin_substep()
+    done = 0
+    t0 = time.perf_counter()
+    ncol = s.n_colors()
+    c = 0
+    while True:
+        s.iterate_color(c % ncol)
+        done += s.color_size(c % ncol)
+        c += 1
+        if time.perf_counter() - t0 >= target_s and c >= ncol:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{c} colour phases ({done} vertex-solves, {c / ncol:.2f} sweeps) of the 513x513 cloth, "
+                      f"full-element FP64 AD per incidence, {dt:.1f} s"}
+
+
+def run_reference(args, dist, rank, local, ws):
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    w = 2.0
+    obj = O.build_spring_cloth(0.1 * w * w, w, w, ROWS, ROWS, 1e4, 1e-4, 1e5, 0.1, 12345)
+    s = O.Vbd(obj, DT, 1, ITERATIONS, GRAVITY, O.FULL_AD)
+    s.begin_substep()
+    ncol = s.n_colors()
+    for k in range(args.warmup):
+        s.iterate_color(k % ncol)
+    times, done = [], 0
+    for k in range(args.steps):
+        c = (args.warmup + k) % ncol
+        t0 = time.perf_counter()
+        s.iterate_color(c)
+        times.append(time.perf_counter() - t0)
+        done += s.color_size(c)
+    total = sum(times)
+    value = done / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "parallelism": "host OpenMP"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"each step = one colour phase of one VBD iteration (colours cycled), "
+                                       f"{done} vertex-solves in total, full-element FP64 AD per incidence"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, dist, rank, local, ws):
+    import numpy as np
+
+    from spg_gb300 import native as N
+    from spg_gb300 import scenes as S
+
+    scene = S.spring_cloth(ROWS)
+    obj = scene.objects[0]
+    solver = N.VbdSolver([obj], dt=DT, iterations=ITERATIONS, gravity=GRAVITY, device=local,
+                         lanes_per_vertex=args.lanes, block_size=args.block)
+    lanes, block = solver.launch()
+    nv = obj.nv
+
+    import torch
+    dev = torch.device(f"cuda:{local}")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
+
+    for _ in range(args.warmup):
+        solver.step()
+    sampler = ClockSampler(local)
+    _barrier(dist, local)
+    torch.cuda.synchronize(dev)
+    sampler.start()
+    t_wall0 = time.perf_counter()
+    dev_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize(dev)
+        st = solver.step()
+        dev_ms.append(st.device_ms)
+    torch.cuda.synchronize(dev)
+    _barrier(dist, local)
+    wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    dev_total_s = _max_over_ranks(dist, local, sum(dev_ms) * 1e-3)
+    solves = _sum_over_ranks(dist, local, float(nv * ITERATIONS * args.steps))
+    value = solves / dev_total_s
+    launches_per_step = 2 + ITERATIONS * solver.n_colors(-1)
+
+    # End-to-end through the C ABI with host buffers: upload state, step, download state.
+    x_host, v_host = solver.state(0)
+    x_host = np.ascontiguousarray(x_host)
+    v_host = np.ascontiguousarray(v_host)
+    e2e_steps = max(1, min(args.steps, 10))
+    _barrier(dist, local)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        solver.set_state(0, x_host, v_host)
+        solver.step()
+        solver.get_state_into(0, x_host, v_host)
+    _barrier(dist, local)
+    e2e_s = _max_over_ranks(dist, local, time.perf_counter() - t0)
+    e2e_value = _sum_over_ranks(dist, local, float(nv * ITERATIONS * e2e_steps)) / e2e_s
+    bytes_state = nv * (2 * 16 + 16)  # base + delta + velocity float4 per vertex
+
+    # Roofline of the dominant kernel (the per-colour VBD kernel): CUDA events around every
+    # colour launch on the solver's stream.
+    color_ms = solver.profile_sweeps(5)
+    sweep_s = float(color_ms.sum()) * 1e-3
+    alg_bytes = algorithmic_bytes_per_iteration(obj)
+    peak, peak_kind = _measured_peaks()
+    achieved = alg_bytes / sweep_s / 1e9
+    traffic = _traffic_per_iteration()
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_total_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB write)",
+                   "lanes_per_vertex": lanes, "block_size": block, "colors": int(solver.n_colors(-1)),
+                   "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
+        "gpu_launches": launches_per_step * args.steps,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
+                "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "vbd_color_kernel", "algorithmic_bytes_per_sweep": alg_bytes,
+                     "bytes_per_vertex_solve": alg_bytes / nv, "sweep_ms": 1e3 * sweep_s,
+                     "color_launch_ms": [round(float(c), 5) for c in color_ms]},
+        "clocks": clocks,
+    }
+    if ws == 1 and not args.skip_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
+    ap.add_argument("--block", type=int, default=0, help="threads per block (0 = autotune)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    dist, rank, local, ws = _dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist, rank, local, ws)
+        return run_gb300(args, dist, rank, local, ws)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

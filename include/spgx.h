@@ -1,0 +1,232 @@
+/*
+ * spgx.h — C ABI of the GB300 (sm_103a) Vertex Block Descent and XPBD solvers.
+ *
+ * This is the drop-in boundary for SPG's solver plugin point. A host C++ adapter that
+ * derives from spg::solver::BaseSolver (spg/include/spg/sim/solver/baseSolver.h:14-41)
+ * packs each ParticleGroup and its energies into an spgx_scene_desc and forwards step()
+ * to spgx_vbd_step() / spgx_xpbd_step(). Plain pointers and sizes only; no C++ or CUDA
+ * types cross this boundary and no exception escapes it.
+ *
+ * Reference interfaces replaced (paths inside the spg project):
+ *   spgx_vbd_*   spg::solver::VBD   spg/include/spg/sim/solver/vbd.h:14-41,
+ *                                   spg/source/sim/solver/vbd.cpp:12-268
+ *   spgx_xpbd_*  spg::solver::XPBD  spg/include/spg/sim/solver/xpbd.h:13-27,
+ *                                   spg/source/sim/solver/xpbd.cpp:16-160
+ *   spgx_energy_desc   the five Energy<ParticleGroup> implementations on the hot path and
+ *                      their precomputed per-stencil data (energy.h:21-369)
+ *
+ * Threading: a handle owns one CUDA stream; calls on one handle must be serialised by the
+ * caller (the reference solvers are not re-entrant either). Distinct handles are
+ * independent. Every call returns after its GPU work has finished unless stated otherwise.
+ */
+#ifndef SPGX_H
+#define SPGX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPGX_API_VERSION 1
+
+typedef enum spgx_status {
+    SPGX_OK = 0,
+    SPGX_ERR_INVALID_ARG = 1,        /* mirrors the reference's setup-time std::runtime_error */
+    SPGX_ERR_UNSUPPORTED_ENERGY = 2, /* energy type outside the five below */
+    SPGX_ERR_CUDA = 3,               /* CUDA runtime error (message in spgx_last_error_string) */
+    SPGX_ERR_NONFINITE = 4,          /* a vertex update produced NaN/Inf; the update was not stored */
+    SPGX_ERR_TIMEOUT = 5,            /* a bounded device-side wait gave up */
+    SPGX_ERR_NO_DEVICE = 6           /* no CUDA device, or not an sm_103 device */
+} spgx_status;
+
+/* Energy types (the reference classes whose precomputed data the params carry). */
+typedef enum spgx_energy_type {
+    SPGX_ENERGY_SPRING = 1,             /* spg::SpringEnergy             springEnergy.h:9 */
+    SPGX_ENERGY_SPRING_ANCHOR = 2,      /* spg::SpringAnchorEnergy       springAnchorEnergy.h:7 */
+    SPGX_ENERGY_DISCRETE_BENDING = 3,   /* spg::DiscreteBendingEnergy    discreteBendingEnergy.h:9 */
+    SPGX_ENERGY_MEMBRANE_STVK = 4,      /* spg::MembraneStvkEnergy       membraneStvkEnergy.h:9 */
+    SPGX_ENERGY_STABLE_NEO_HOOKEAN = 5  /* spg::StableNeoHookeanEnergy   stableNeoHookeanEnergy.h:10 */
+} spgx_energy_type;
+
+/*
+ * One energy: n_stencils stencils of spgx_stencil_size(type) vertex indices each (the
+ * reference's flatStencils(), energy.h:102-110) and spgx_param_count(type) doubles per
+ * stencil, in this order:
+ *   SPRING            [restLength, effectiveStiffness, effectiveCompliance]
+ *   SPRING_ANCHOR     [anchor.x, anchor.y, anchor.z, modelStiffness, effectiveCompliance]
+ *   DISCRETE_BENDING  [restTheta, effectiveStiffness, effectiveCompliance]
+ *   MEMBRANE_STVK     [inverseReferenceMat (2x2 row-major), effectiveStiffness (3x3 row-major),
+ *                      effectiveCompliance (3x3 row-major)]
+ *   STABLE_NEO_HOOKEAN [inverseReferenceMat (3x3 row-major), effectiveStiffness(0,0),
+ *                      effectiveStiffness(1,1), hydrostaticCorrectionTerm,
+ *                      effectiveCompliance(0,0), effectiveCompliance(1,1)]
+ * i.e. the values the reference holds after addStencil() and preparePrecomputations().
+ */
+typedef struct spgx_energy_desc {
+    int32_t type;
+    int32_t n_stencils;
+    const int32_t *stencils;
+    const double *params;
+} spgx_energy_desc;
+
+/* One ParticleGroup (particleGroup.h:14-60): positions, velocities (NULL = zero), masses. */
+typedef struct spgx_object_desc {
+    int32_t n_vertices;
+    const double *x;    /* 3 * n_vertices */
+    const double *v;    /* 3 * n_vertices or NULL */
+    const double *mass; /* n_vertices */
+    int32_t n_energies;
+    const spgx_energy_desc *energies; /* in obj.energies() order */
+} spgx_object_desc;
+
+/* A solver's object list (BaseSolver::m_objects particle groups). Objects are independent
+ * and are solved together, colour by colour, in one launch per colour. */
+typedef struct spgx_scene_desc {
+    int32_t n_objects;
+    const spgx_object_desc *objects;
+} spgx_scene_desc;
+
+int32_t spgx_stencil_size(int32_t type);
+int32_t spgx_param_count(int32_t type);
+int32_t spgx_api_version(void);
+
+/* Last error message of the calling thread ("" if none). */
+const char *spgx_last_error_string(void);
+
+/* ------------------------------------------------------------------------------------ */
+/* Host-only setup (no device needed)                                                     */
+
+/* Greedy vertex colouring of one object, bit-exact with coloring::colorVertices
+ * (graphColoring.cpp:72-84 -> Graph::greedyColoring :21-49). colors: n_vertices. */
+spgx_status spgx_color_vertices(const spgx_object_desc *obj, int32_t *colors);
+/* Greedy stencil colouring of one energy, bit-exact with coloring::colorStencils
+ * (graphColoring.cpp:51-70). colors: n_stencils. */
+spgx_status spgx_color_stencils(const spgx_energy_desc *energy, int32_t *colors);
+/* Per-vertex incidence lists of one object in reference order (VBD::computeStencilInfoPerVertex,
+ * vbd.cpp:231-268): counts[v * n_energies + e] and (stencilIdx, vertexIdxInStencil) pairs. */
+spgx_status spgx_incidences(const spgx_object_desc *obj, int32_t *counts, int32_t *entries, int64_t *total);
+
+/* ------------------------------------------------------------------------------------ */
+/* Vertex Block Descent                                                                  */
+
+typedef struct spgx_vbd spgx_vbd;
+
+typedef struct spgx_vbd_params {
+    double dt;                 /* BaseSolver::setDt (baseSolver.h:26) */
+    int32_t substeps;          /* BaseSolver::setNumSubsteps (baseSolver.h:28) */
+    int32_t iterations;        /* VBD::m_iterations (vbd.h:33; fixed at 1 in the reference) */
+    double gravity[3];         /* BaseSolver::setGravity (baseSolver.h:32) */
+    double tolerance;          /* > 0: iterate until ||r|| <= tolerance * ||r(y)||, see below */
+    int32_t max_iterations;    /* cap per substep when tolerance > 0 */
+    int32_t check_interval;    /* iterations between residual checks when tolerance > 0 */
+    double fallback_condition; /* 3x3 blocks whose condition estimate exceeds this are solved in FP64 */
+    int32_t lanes_per_vertex;  /* 0 = autotune; else 1, 2, 4, 8, 16 or 32 */
+    int32_t block_size;        /* 0 = autotune; else a multiple of 32 up to 1024 */
+    int32_t use_graph;         /* 1 = replay the iteration loop as a CUDA graph */
+    int32_t device;            /* CUDA device ordinal */
+} spgx_vbd_params;
+
+/* Defaults: dt 0.01, 1 substep, 1 iteration, gravity (0,-9.8,0) (baseSolver.h:36-38),
+ * tolerance 0, max_iterations 1000, check_interval 10, fallback_condition 1e6, autotune,
+ * use_graph 1, device 0. */
+void spgx_vbd_params_default(spgx_vbd_params *p);
+
+typedef struct spgx_step_stats {
+    int32_t iterations;        /* VBD iterations run in the step, summed over substeps */
+    int32_t fallback_solves;   /* 3x3 solves redone in FP64 */
+    int32_t skipped_solves;    /* vertices skipped by the det(H) > 1e-10 guard (vbd.cpp:139) */
+    int32_t converged;         /* tolerance mode: every substep reached the tolerance */
+    double residual_initial;   /* ||r(y)|| of the last substep (tolerance mode, else 0) */
+    double residual_final;     /* ||r(x)|| at the end of the last substep (tolerance mode) */
+    double device_ms;          /* CUDA-event time of the step on the handle's stream */
+} spgx_step_stats;
+
+/*
+ * Creates a solver for the scene. The scene is copied (positions become FP32 on the device,
+ * element data FP32); the caller keeps ownership of every array. Setup mirrors the
+ * reference's first step(): greedy vertex colouring per object (vbd.cpp:203-229, bit-exact
+ * with graphColoring.cpp:21-84) and the per-vertex incidence lists (vbd.cpp:231-268).
+ */
+spgx_status spgx_vbd_create(const spgx_scene_desc *scene, const spgx_vbd_params *params, spgx_vbd **out);
+spgx_status spgx_vbd_destroy(spgx_vbd *h);
+spgx_status spgx_vbd_set_params(spgx_vbd *h, const spgx_vbd_params *params);
+
+/*
+ * One VBD::step() (vbd.cpp:12-195) for every object: per substep, inertial prediction,
+ * `iterations` colour sweeps of per-vertex 3x3 Newton updates (or, with tolerance > 0, sweeps
+ * until the incremental-potential residual r = M/h^2 (x - y) + grad E(x), reduced in FP64,
+ * satisfies ||r|| <= tolerance * ||r(y)||), then the velocity update. stats may be NULL.
+ */
+spgx_status spgx_vbd_step(spgx_vbd *h, spgx_step_stats *stats);
+
+/* Host <-> device state of one object (3 * n_vertices doubles each; NULL skips). */
+spgx_status spgx_vbd_get_state(spgx_vbd *h, int32_t object, double *x, double *v);
+spgx_status spgx_vbd_set_state(spgx_vbd *h, int32_t object, const double *x, const double *v);
+
+/* BaseSolver::reset (baseSolver.cpp:23-32): positions back to those given at create,
+ * velocities to zero. */
+spgx_status spgx_vbd_reset(spgx_vbd *h);
+
+/* FP64-reduced residual norm over all objects at the current state against the inertial
+ * target of the most recent substep (zero target before the first step). */
+spgx_status spgx_vbd_residual(spgx_vbd *h, double *norm);
+
+/* Introspection for parity checks. object -1 gives the number of colour phases of the
+ * whole scene (the maximum over objects). */
+spgx_status spgx_vbd_num_colors(spgx_vbd *h, int32_t object, int32_t *n);
+spgx_status spgx_vbd_get_colors(spgx_vbd *h, int32_t object, int32_t *colors);
+/* Incidence lists in reference order: counts[v * n_energies + e] and, in the same order,
+ * (stencilIdx, vertexIdxInStencil) pairs. Pass entries == NULL to query *total first. */
+spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts, int32_t *entries, int64_t *total);
+/* Launch configuration the solver uses (after autotuning). */
+spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *lanes_per_vertex, int32_t *block_size);
+/* Runs `iterations` colour sweeps with a CUDA event pair around every colour launch on the
+ * handle's stream and writes the mean duration (ms) of each colour's launch to color_ms
+ * (spgx_vbd_num_colors(h, -1, ...) entries). Advances the positions like the iterations of
+ * a step (no inertial or velocity phase). */
+spgx_status spgx_vbd_profile_sweeps(spgx_vbd *h, int32_t iterations, double *color_ms);
+
+/* ------------------------------------------------------------------------------------ */
+/* Element-level evaluation on the GPU with the solver's device code (FP32), for the
+ * per-element derivative parity checks. For n incidences of one energy type:
+ * X = n * stencil_size * 3 positions, params = n * param_count, slots = n vertex slots.
+ * grad = n * 3 (energy gradient segment of the slot), hess = n * 9 (row-major 3x3 block). */
+spgx_status spgx_eval_vertex_blocks(int32_t type, int32_t n, const double *X, const double *params,
+                                    const int32_t *slots, double *grad, double *hess);
+/* Constraint values (n * nc) and gradients (n * nc * 3 * stencil_size, constraint-major)
+ * as used by the XPBD projection. */
+spgx_status spgx_eval_constraints(int32_t type, int32_t n, const double *X, const double *params, double *C,
+                                  double *gradC);
+int32_t spgx_num_constraints(int32_t type);
+
+/* ------------------------------------------------------------------------------------ */
+/* XPBD (one projection sweep per substep, xpbd.h:13-15)                                  */
+
+typedef struct spgx_xpbd spgx_xpbd;
+
+typedef struct spgx_xpbd_params {
+    double dt;
+    int32_t substeps;
+    double gravity[3];
+    int32_t block_size; /* 0 = default */
+    int32_t use_graph;
+    int32_t device;
+} spgx_xpbd_params;
+
+void spgx_xpbd_params_default(spgx_xpbd_params *p);
+spgx_status spgx_xpbd_create(const spgx_scene_desc *scene, const spgx_xpbd_params *params, spgx_xpbd **out);
+spgx_status spgx_xpbd_destroy(spgx_xpbd *h);
+spgx_status spgx_xpbd_set_params(spgx_xpbd *h, const spgx_xpbd_params *params);
+spgx_status spgx_xpbd_step(spgx_xpbd *h, spgx_step_stats *stats);
+spgx_status spgx_xpbd_get_state(spgx_xpbd *h, int32_t object, double *x, double *v);
+spgx_status spgx_xpbd_set_state(spgx_xpbd *h, int32_t object, const double *x, const double *v);
+spgx_status spgx_xpbd_reset(spgx_xpbd *h);
+/* Stencil colours of one energy (colorStencils, graphColoring.cpp:51-70). */
+spgx_status spgx_xpbd_get_stencil_colors(spgx_xpbd *h, int32_t object, int32_t energy, int32_t *colors);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPGX_H */

@@ -1,0 +1,213 @@
+// Device-side views of the solver state and element tables, and the per-vertex incidence
+// accumulation shared by the VBD colour kernel and the residual kernel.
+//
+// State layout (internal, colour-major vertex order):
+//   pos[2 v]     base position of the current step (x_n, FP32), w unused
+//   pos[2 v + 1] delta from the base (x = base + delta), w unused
+//   tgt[v]       inertial target as a delta from the base (y - base), w = mass
+//   dold[v]      delta of x_old (the position at the start of the substep)
+//   vel[v]       velocity
+// Element evaluation subtracts bases and deltas separately, relative to the vertex being
+// solved, so FP32 resolves the within-step motion far below the ulp of absolute positions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "elements.cuh"
+
+namespace spgx {
+
+struct DevTables {
+    const float4 *anchors;
+    const int4 *springs;
+    const float *spring_cmp;
+    const int4 *bend_idx;
+    const float4 *bend_prm;
+    const int4 *stvk_idx;
+    const float4 *stvk_D;
+    const float4 *stvk_Ka;
+    const float4 *stvk_Kb;
+    const float4 *stvk_Ca;
+    const float4 *stvk_Cb;
+    const float *stvk_Cc;
+    const int4 *snh_idx;
+    const float4 *snh_p0;
+    const float4 *snh_p1;
+    const float4 *snh_p2;
+    const float2 *snh_cmp;
+    const float2 *anchor_cmp;
+};
+
+struct DevState {
+    float4 *pos;
+    float4 *tgt;
+    float4 *dold;
+    float4 *vel;
+    const int4 *hdr;
+    const int *adj;
+    int *counters;          // [0] FP64 fallback solves, [1] det-guard skips
+    unsigned int *status;   // bit 0: non-finite update
+};
+
+typedef Vec3<float> V3f;
+
+__device__ __forceinline__ V3f v3(float4 a) { return mk(a.x, a.y, a.z); }
+
+// Position of vertex j relative to the vertex whose base/delta are (bs, ds).
+__device__ __forceinline__ V3f rel_pos(const float4 *__restrict__ pos, int j, V3f bs, V3f ds)
+{
+    const float4 b = __ldg(pos + 2 * j);
+    const float4 d = __ldg(pos + 2 * j + 1);
+    return mk((b.x - bs.x) + (d.x - ds.x), (b.y - bs.y) + (d.y - ds.y), (b.z - bs.z) + (d.z - ds.z));
+}
+
+__device__ __forceinline__ int warp_max(int v) { return __reduce_max_sync(0xffffffffu, v); }
+
+// Walks the vertex's class-sorted incidence list with G lanes per vertex (lane-strided) and
+// accumulates the force and Hessian block of every incident element into acc.
+// Loop trip counts are warp-uniform (max over the warp), so all 32 lanes stay converged.
+template <int G>
+__device__ __forceinline__ void accumulate_incidences(const DevTables &T, const float4 *__restrict__ pos,
+                                                      const int *__restrict__ adj, int4 h, int lane, V3f bs, V3f ds,
+                                                      Block<float> &acc)
+{
+    int off = h.x;
+    const V3f zero = mk(0.f, 0.f, 0.f);
+    // Anchors
+    {
+        const int n = h.y & 0xffff;
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int e = __ldg(adj + off + i) >> 2;
+                const float4 a = __ldg(T.anchors + e);
+                const V3f xa = mk((bs.x - a.x) + ds.x, (bs.y - a.y) + ds.y, (bs.z - a.z) + ds.z);
+                anchor_block(xa, zero, a.w, acc);
+            }
+        }
+        off += n;
+    }
+    // Springs
+    {
+        const int n = (h.y >> 16) & 0xffff;
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int ent = __ldg(adj + off + i);
+                const int4 s = __ldg(T.springs + (ent >> 2));
+                const int o = (ent & 3) ? s.x : s.y;
+                const V3f po = rel_pos(pos, o, bs, ds);
+                spring_block(zero, po, __int_as_float(s.z), __int_as_float(s.w), acc);
+            }
+        }
+        off += n;
+    }
+    // Bending, flap vertices (slots 2, 3)
+    {
+        const int n = h.z & 0xffff;
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int ent = __ldg(adj + off + i);
+                const int e = ent >> 2;
+                const int slot = ent & 3;
+                const int4 st = __ldg(T.bend_idx + e);
+                const float4 pr = __ldg(T.bend_prm + e);
+                const V3f p0 = rel_pos(pos, st.x, bs, ds);
+                const V3f p1 = rel_pos(pos, st.y, bs, ds);
+                const V3f po = rel_pos(pos, slot == 2 ? st.w : st.z, bs, ds);
+                bending_flap_block(p0, p1, zero, po, slot == 2 ? pr.x : -pr.x, pr.y, acc);
+            }
+        }
+        off += n;
+    }
+    // Bending, hinge vertices (slots 0, 1)
+    {
+        const int n = (h.z >> 16) & 0xffff;
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int ent = __ldg(adj + off + i);
+                const int e = ent >> 2;
+                const int slot = ent & 3;
+                const int4 st = __ldg(T.bend_idx + e);
+                const float4 pr = __ldg(T.bend_prm + e);
+                const V3f po = rel_pos(pos, slot == 1 ? st.x : st.y, bs, ds);
+                const V3f pa = rel_pos(pos, st.z, bs, ds);
+                const V3f pb = rel_pos(pos, st.w, bs, ds);
+                bending_hinge_block(po, zero, pa, pb, slot == 1 ? pr.x : -pr.x, pr.y, acc);
+            }
+        }
+        off += n;
+    }
+    // StVK membrane
+    {
+        const int n = h.w & 0xffff;
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int ent = __ldg(adj + off + i);
+                const int e = ent >> 2;
+                const int slot = ent & 3;
+                const int4 st = __ldg(T.stvk_idx + e);
+                const float4 D4 = __ldg(T.stvk_D + e);
+                const float4 Ka = __ldg(T.stvk_Ka + e);
+                const float4 Kb = __ldg(T.stvk_Kb + e);
+                V3f p[3];
+                p[0] = slot == 0 ? zero : rel_pos(pos, st.x, bs, ds);
+                p[1] = slot == 1 ? zero : rel_pos(pos, st.y, bs, ds);
+                p[2] = slot == 2 ? zero : rel_pos(pos, st.z, bs, ds);
+                const float D[4] = {D4.x, D4.y, D4.z, D4.w};
+                const float Ks[6] = {Ka.x, Ka.y, Ka.z, Ka.w, Kb.x, Kb.y};
+                stvk_block(p, slot, D, Ks, acc);
+            }
+        }
+        off += n;
+    }
+    // Stable Neo-Hookean
+    {
+        const int n = (h.w >> 16) & 0xffff;
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int ent = __ldg(adj + off + i);
+                const int e = ent >> 2;
+                const int slot = ent & 3;
+                const int4 st = __ldg(T.snh_idx + e);
+                const float4 a = __ldg(T.snh_p0 + e);
+                const float4 b = __ldg(T.snh_p1 + e);
+                const float4 c = __ldg(T.snh_p2 + e);
+                V3f p[4];
+                p[0] = slot == 0 ? zero : rel_pos(pos, st.x, bs, ds);
+                p[1] = slot == 1 ? zero : rel_pos(pos, st.y, bs, ds);
+                p[2] = slot == 2 ? zero : rel_pos(pos, st.z, bs, ds);
+                p[3] = slot == 3 ? zero : rel_pos(pos, st.w, bs, ds);
+                const float D[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+                snh_block(p, slot, D, c.y, c.z, c.w, acc);
+            }
+        }
+    }
+}
+
+// Sum of the 9 block entries over the G lanes of a vertex group (xor butterfly; every lane
+// ends with the total).
+template <int G>
+__device__ __forceinline__ void group_reduce(Block<float> &acc)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc.f[k] += __shfl_xor_sync(0xffffffffu, acc.f[k], o);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc.h[k] += __shfl_xor_sync(0xffffffffu, acc.h[k], o);
+    }
+}
+
+}  // namespace spgx

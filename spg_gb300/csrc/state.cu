@@ -1,0 +1,183 @@
+// Particle state management and the substep kernels shared by VBD and XPBD.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "api_internal.h"
+#include "state.h"
+
+namespace spgx {
+
+// Inertial prediction shared by VBD (vbd.cpp:46-83) and XPBD (xpbd.cpp:44-74):
+// v += h g; x_old = x; x += h v (and, for VBD, y = x). The base first advances to
+// fl(base + delta) with the exact two-sum remainder kept as the new delta, so
+// x_old = base + dold holds exactly.
+__global__ void begin_substep_kernel(float4 *pos, float4 *tgt, float4 *dold, float4 *vel, int nv, float h, float gx,
+                                     float gy, float gz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float4 b = pos[2 * i];
+    const float4 d = pos[2 * i + 1];
+    float4 v = vel[i];
+    const float mass = tgt[i].w;
+    float s[3], r[3];
+    const float bb[3] = {b.x, b.y, b.z}, dd[3] = {d.x, d.y, d.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        s[k] = bb[k] + dd[k];
+        const float t = s[k] - bb[k];
+        r[k] = (bb[k] - (s[k] - t)) + (dd[k] - t);
+    }
+    v.x += h * gx;
+    v.y += h * gy;
+    v.z += h * gz;
+    const float4 y = make_float4(r[0] + h * v.x, r[1] + h * v.y, r[2] + h * v.z, 0.f);
+    pos[2 * i] = make_float4(s[0], s[1], s[2], b.w);
+    pos[2 * i + 1] = y;
+    dold[i] = make_float4(r[0], r[1], r[2], 0.f);
+    tgt[i] = make_float4(y.x, y.y, y.z, mass);
+    vel[i] = v;
+}
+
+// Velocity update (vbd.cpp:174-185, xpbd.cpp:111-120 -> particleGroup.cpp:65-72):
+// v = (x - x_old) / h.
+__global__ void end_substep_kernel(const float4 *pos, const float4 *dold, float4 *vel, int nv, float invh)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float4 d = pos[2 * i + 1];
+    const float4 o = dold[i];
+    vel[i] = make_float4((d.x - o.x) * invh, (d.y - o.y) * invh, (d.z - o.z) * invh, 0.f);
+}
+
+void launch_begin_substep(const ParticleState &P, double h, const double *g, cudaStream_t st)
+{
+    if (P.nv == 0) return;
+    begin_substep_kernel<<<(P.nv + 255) / 256, 256, 0, st>>>(P.pos(), P.tgt(), P.dold(), P.vel(), P.nv, float(h),
+                                                             float(g[0]), float(g[1]), float(g[2]));
+}
+
+void launch_end_substep(const ParticleState &P, double h, cudaStream_t st)
+{
+    if (P.nv == 0) return;
+    end_substep_kernel<<<(P.nv + 255) / 256, 256, 0, st>>>(P.pos(), P.dold(), P.vel(), P.nv, float(1.0 / h));
+}
+
+spgx_status ParticleState::init(const SceneLayout &L)
+{
+    nv = L.nv;
+    const size_t n = size_t(nv);
+    SPGX_TRY_STATUS(d_pos.alloc(n * 2 * sizeof(float4)));
+    SPGX_TRY_STATUS(d_tgt.alloc(n * sizeof(float4)));
+    SPGX_TRY_STATUS(d_dold.alloc(n * sizeof(float4)));
+    SPGX_TRY_STATUS(d_vel.alloc(n * sizeof(float4)));
+    SPGX_TRY_STATUS(h_pos.alloc(n * 2 * sizeof(float4)));
+    SPGX_TRY_STATUS(h_vel.alloc(n * sizeof(float4)));
+    std::vector<float4> tg(n);
+    std::vector<float> invm(n);
+    float4 *hp = h_pos.as<float4>();
+    float4 *hv = h_vel.as<float4>();
+    for (size_t ext = 0; ext < n; ++ext) {
+        const int i = L.ext2int[ext];
+        const double *x = &L.x_ext[3 * ext];
+        const double *v = &L.v_ext[3 * ext];
+        const float bx = float(x[0]), by = float(x[1]), bz = float(x[2]);
+        hp[2 * i] = make_float4(bx, by, bz, 0.f);
+        hp[2 * i + 1] = make_float4(float(x[0] - bx), float(x[1] - by), float(x[2] - bz), 0.f);
+        hv[i] = make_float4(float(v[0]), float(v[1]), float(v[2]), 0.f);
+        tg[i] = make_float4(hp[2 * i + 1].x, hp[2 * i + 1].y, hp[2 * i + 1].z, L.mass[i]);
+        // ParticleGroup::addParticle: w = (m == 0 ? 0 : 1 / m), particleGroup.cpp:81
+        invm[i] = L.mass[i] == 0.f ? 0.f : 1.f / L.mass[i];
+    }
+    SPGX_CUDA(cudaMemcpy(pos(), hp, n * 2 * sizeof(float4), cudaMemcpyHostToDevice));
+    SPGX_CUDA(cudaMemcpy(vel(), hv, n * sizeof(float4), cudaMemcpyHostToDevice));
+    SPGX_CUDA(cudaMemcpy(tgt(), tg.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    SPGX_CUDA(cudaMemset(dold(), 0, n * sizeof(float4)));
+    SPGX_TRY_STATUS(d_invm.upload(invm));
+    host_valid = true;
+    device_dirty = false;
+    return SPGX_OK;
+}
+
+spgx_status ParticleState::upload_if_dirty(cudaStream_t stream)
+{
+    if (!device_dirty) return SPGX_OK;
+    const size_t n = size_t(nv);
+    SPGX_CUDA(cudaMemcpyAsync(pos(), h_pos.as<void>(), n * 2 * sizeof(float4), cudaMemcpyHostToDevice, stream));
+    SPGX_CUDA(cudaMemcpyAsync(vel(), h_vel.as<void>(), n * sizeof(float4), cudaMemcpyHostToDevice, stream));
+    device_dirty = false;
+    return SPGX_OK;
+}
+
+spgx_status ParticleState::download_if_stale(cudaStream_t stream)
+{
+    if (host_valid) return SPGX_OK;
+    const size_t n = size_t(nv);
+    SPGX_CUDA(cudaMemcpyAsync(h_pos.as<void>(), pos(), n * 2 * sizeof(float4), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaMemcpyAsync(h_vel.as<void>(), vel(), n * sizeof(float4), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    host_valid = true;
+    return SPGX_OK;
+}
+
+spgx_status ParticleState::get(const SceneLayout &L, int obj, double *x, double *v, cudaStream_t stream)
+{
+    if (obj < 0 || obj >= static_cast<int>(L.objects.size())) {
+        set_error("invalid object index");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_TRY_STATUS(download_if_stale(stream));
+    const auto &O = L.objects[obj];
+    const float4 *hp = h_pos.as<float4>();
+    const float4 *hv = h_vel.as<float4>();
+    for (int k = 0; k < O.nv; ++k) {
+        const int i = L.ext2int[O.vertex_base + k];
+        if (x) {
+            x[3 * k + 0] = double(hp[2 * i].x) + double(hp[2 * i + 1].x);
+            x[3 * k + 1] = double(hp[2 * i].y) + double(hp[2 * i + 1].y);
+            x[3 * k + 2] = double(hp[2 * i].z) + double(hp[2 * i + 1].z);
+        }
+        if (v) {
+            v[3 * k + 0] = hv[i].x;
+            v[3 * k + 1] = hv[i].y;
+            v[3 * k + 2] = hv[i].z;
+        }
+    }
+    return SPGX_OK;
+}
+
+spgx_status ParticleState::set(const SceneLayout &L, int obj, const double *x, const double *v, cudaStream_t stream)
+{
+    if (obj < 0 || obj >= static_cast<int>(L.objects.size())) {
+        set_error("invalid object index");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_TRY_STATUS(download_if_stale(stream));
+    const auto &O = L.objects[obj];
+    float4 *hp = h_pos.as<float4>();
+    float4 *hv = h_vel.as<float4>();
+    for (int k = 0; k < O.nv; ++k) {
+        const int i = L.ext2int[O.vertex_base + k];
+        if (x) {
+            const float bx = float(x[3 * k]), by = float(x[3 * k + 1]), bz = float(x[3 * k + 2]);
+            hp[2 * i] = make_float4(bx, by, bz, 0.f);
+            hp[2 * i + 1] =
+                make_float4(float(x[3 * k] - bx), float(x[3 * k + 1] - by), float(x[3 * k + 2] - bz), 0.f);
+        }
+        if (v) hv[i] = make_float4(float(v[3 * k]), float(v[3 * k + 1]), float(v[3 * k + 2]), 0.f);
+    }
+    device_dirty = true;
+    return SPGX_OK;
+}
+
+spgx_status ParticleState::reset(const SceneLayout &L, cudaStream_t stream)
+{
+    for (int o = 0; o < static_cast<int>(L.objects.size()); ++o) {
+        const std::vector<double> zeros(L.objects[o].x_init.size(), 0.0);
+        SPGX_TRY_STATUS(set(L, o, L.objects[o].x_init.data(), zeros.data(), stream));
+    }
+    return SPGX_OK;
+}
+
+}  // namespace spgx

