@@ -235,8 +235,8 @@ def run_gb300(args, dist, rank, local, ws):
     scene = S.spring_cloth(ROWS)
     obj = scene.objects[0]
     solver = N.VbdSolver([obj], dt=DT, iterations=ITERATIONS, gravity=GRAVITY, device=local,
-                         lanes_per_vertex=args.lanes, block_size=args.block)
-    lanes, block = solver.launch()
+                         lanes_per_vertex=args.lanes, block_size=args.block, kernel=args.kernel)
+    kernel, lanes, block = solver.launch()
     nv = obj.nv
 
     import torch
@@ -297,14 +297,17 @@ def run_gb300(args, dist, rank, local, ws):
         "ms_per_step": 1e3 * dev_total_s / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB write)",
-                   "lanes_per_vertex": lanes, "block_size": block, "colors": int(solver.n_colors(-1)),
+                   "kernel": {1: "lanes-per-vertex", 2: "shared-memory tiles"}[kernel],
+                   "lanes_per_vertex" if kernel == 1 else "tile_vertices": lanes, "block_size": block,
+                   "colors": int(solver.n_colors(-1)),
                    "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
         "gpu_launches": launches_per_step * args.steps,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
                 "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "vbd_color_kernel", "algorithmic_bytes_per_sweep": alg_bytes,
+                     "kernel": "vbd_color_kernel" if kernel == 1 else "vbd_tile_kernel",
+                     "algorithmic_bytes_per_sweep": alg_bytes,
                      "bytes_per_vertex_solve": alg_bytes / nv, "sweep_ms": 1e3 * sweep_s,
                      "color_launch_ms": [round(float(c), 5) for c in color_ms]},
         "clocks": clocks,
@@ -324,6 +327,7 @@ def main():
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0 = autotune)")
+    ap.add_argument("--kernel", type=int, default=0, help="1 = lanes per vertex, 2 = tiles (0 = autotune)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -122,14 +122,16 @@ typedef struct spgx_vbd_params {
     int32_t check_interval;    /* iterations between residual checks when tolerance > 0 */
     double fallback_condition; /* 3x3 blocks whose condition estimate exceeds this are solved in FP64 */
     int32_t lanes_per_vertex;  /* 0 = autotune; else 1, 2, 4, 8, 16 or 32 */
-    int32_t block_size;        /* 0 = autotune; else a multiple of 32 up to 1024 */
+    int32_t block_size;        /* 0 = autotune; else a multiple of 32 up to 256 (lanes kernel) */
     int32_t use_graph;         /* 1 = replay the iteration loop as a CUDA graph */
     int32_t device;            /* CUDA device ordinal */
+    int32_t kernel;            /* 0 = autotune, 1 = lanes-per-vertex kernel, 2 = shared-memory tile kernel */
+    int32_t tile_vertices;     /* vertices per tile of the tile kernel (1..128; 0 = 64) */
 } spgx_vbd_params;
 
 /* Defaults: dt 0.01, 1 substep, 1 iteration, gravity (0,-9.8,0) (baseSolver.h:36-38),
  * tolerance 0, max_iterations 1000, check_interval 10, fallback_condition 1e6, autotune,
- * use_graph 1, device 0. */
+ * use_graph 1, device 0, kernel autotune, 64 vertices per tile. */
 void spgx_vbd_params_default(spgx_vbd_params *p);
 
 typedef struct spgx_step_stats {
@@ -179,8 +181,9 @@ spgx_status spgx_vbd_get_colors(spgx_vbd *h, int32_t object, int32_t *colors);
 /* Incidence lists in reference order: counts[v * n_energies + e] and, in the same order,
  * (stencilIdx, vertexIdxInStencil) pairs. Pass entries == NULL to query *total first. */
 spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts, int32_t *entries, int64_t *total);
-/* Launch configuration the solver uses (after autotuning). */
-spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *lanes_per_vertex, int32_t *block_size);
+/* Launch configuration the solver uses (after autotuning): kernel 1 with lanes per vertex and
+ * block size, or kernel 2 (tiles; lanes_per_vertex = vertices per tile, block = threads). */
+spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *kernel, int32_t *lanes_per_vertex, int32_t *block_size);
 /* Runs `iterations` colour sweeps with a CUDA event pair around every colour launch on the
  * handle's stream and writes the mean duration (ms) of each colour's launch to color_ms
  * (spgx_vbd_num_colors(h, -1, ...) entries). Advances the positions like the iterations of

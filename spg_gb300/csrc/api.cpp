@@ -52,6 +52,8 @@ void spgx_vbd_params_default(spgx_vbd_params *p)
     p->block_size = 0;
     p->use_graph = 1;
     p->device = 0;
+    p->kernel = 0;
+    p->tile_vertices = 64;
 }
 
 void spgx_xpbd_params_default(spgx_xpbd_params *p)

@@ -286,8 +286,9 @@ template <typename T>
 SPGX_HD Vec3<T> snh_weights(const T *D, int slot)
 {
     if (slot == 0) return mk(-(D[0] + D[3] + D[6]), -(D[1] + D[4] + D[7]), -(D[2] + D[5] + D[8]));
-    const int r = 3 * (slot - 1);
-    return mk(D[r], D[r + 1], D[r + 2]);
+    if (slot == 1) return mk(D[0], D[1], D[2]);
+    if (slot == 2) return mk(D[3], D[4], D[5]);
+    return mk(D[6], D[7], D[8]);
 }
 
 template <typename T>

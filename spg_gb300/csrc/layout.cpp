@@ -233,18 +233,50 @@ spgx_status build_scene_layout(const spgx_scene_desc *scene, bool with_xpbd, Sce
         base += ob.n_vertices;
     }
 
-    // Colour-major internal order: colour c of every object, objects in order, vertices ascending.
+    // Colour-major internal order. Inside a colour, vertices are grouped by object and ordered
+    // along a Morton curve of their initial positions, so a tile of consecutive same-colour
+    // vertices is spatially compact and its neighbourhoods overlap. The order inside a colour
+    // does not change the result (the colour's vertices are updated independently).
     L.color_start.assign(L.n_colors + 1, 0);
     for (int v = 0; v < nv; ++v) ++L.color_start[color_ext[v] + 1];
     for (int c = 0; c < L.n_colors; ++c) L.color_start[c + 1] += L.color_start[c];
     L.ext2int.resize(nv);
     L.int2ext.resize(nv);
     {
-        std::vector<int32_t> fill(L.color_start.begin(), L.color_start.end() - (L.n_colors > 0 ? 1 : 0));
-        for (int v = 0; v < nv; ++v) {
-            const int i = fill[color_ext[v]]++;
-            L.ext2int[v] = i;
-            L.int2ext[i] = v;
+        std::vector<uint64_t> key(nv);
+        for (int o = 0; o < nobj; ++o) {
+            const auto &OL = L.objects[o];
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (int k = 0; k < OL.nv; ++k)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], OL.x_init[3 * k + a]);
+                    hi[a] = std::max(hi[a], OL.x_init[3 * k + a]);
+                }
+            for (int k = 0; k < OL.nv; ++k) {
+                uint64_t m = 0;
+                uint32_t q[3];
+                for (int a = 0; a < 3; ++a) {
+                    const double ext = hi[a] - lo[a];
+                    const double t = ext > 0 ? (OL.x_init[3 * k + a] - lo[a]) / ext : 0.0;
+                    const double qt = std::min(1023.0, std::max(0.0, std::floor(t * 1023.0 + 0.5)));
+                    q[a] = std::isfinite(qt) ? static_cast<uint32_t>(qt) : 0u;
+                }
+                for (int b = 9; b >= 0; --b)
+                    for (int a = 0; a < 3; ++a) m = (m << 1) | ((q[a] >> b) & 1u);
+                key[OL.vertex_base + k] = (uint64_t(o) << 32) | m;
+            }
+        }
+        std::vector<int32_t> order(nv);
+        {
+            std::vector<int32_t> fill(L.color_start.begin(), L.color_start.end() - (L.n_colors > 0 ? 1 : 0));
+            for (int v = 0; v < nv; ++v) order[fill[color_ext[v]]++] = v;
+        }
+        for (int c = 0; c < L.n_colors; ++c)
+            std::stable_sort(order.begin() + L.color_start[c], order.begin() + L.color_start[c + 1],
+                             [&key](int32_t a, int32_t b) { return key[a] < key[b]; });
+        for (int i = 0; i < nv; ++i) {
+            L.int2ext[i] = order[i];
+            L.ext2int[order[i]] = i;
         }
     }
     L.mass.resize(nv);

@@ -83,6 +83,32 @@ struct SceneLayout {
     double mean_degree{0};
 };
 
+// Tiles of one colour for the shared-memory VBD kernel. A tile is a run of consecutive
+// same-colour vertices (internal order) plus the halo of other vertices its incidences read;
+// its incidences are stored as self-contained records with tile-local vertex indices and
+// inline parameters, class by class, each class in vertex-interleaved order (record r of a
+// class belongs to a different vertex than record r + 1 whenever the tile has several).
+constexpr int kTileMaxLocal = 1024;  // tile vertices + halo vertices
+constexpr int kTileMaxVerts = 128;
+
+struct TileLayout {
+    int tile_vertices{0};
+    int max_local{0};
+    std::vector<int32_t> color_tiles;  // n_colors + 1: tile index range of each colour
+    // Per tile, 4 x I4: {vstart, nvt, halo_off, n_halo}, {off anchor, spring, flap, hinge},
+    // {off stvk, snh, n anchor, n spring}, {n flap, n hinge, n stvk, n snh}.
+    std::vector<I4> hdr;
+    std::vector<int32_t> halo;
+    std::vector<I4> rec_anchor;  // 2 per record
+    std::vector<I4> rec_spring;  // 1
+    std::vector<I4> rec_flap;    // 1
+    std::vector<I4> rec_hinge;   // 1
+    std::vector<I4> rec_stvk;    // 3
+    std::vector<I4> rec_snh;     // 4
+};
+
+spgx_status build_tiles(const SceneLayout &L, int tile_vertices, TileLayout &out, std::string &err);
+
 int stencil_size(int type);
 int param_count(int type);
 

@@ -109,6 +109,59 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
     if (active && lane == 0) solve_and_update(S, v, acc, invdt2, fb2);
 }
 
+// One colour phase with the shared-memory tile kernel: one CTA per tile of the colour.
+__global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V, const DevState S, int tile0,
+                                                                int max_local, int tile_vertices, float invdt2,
+                                                                float fb2)
+{
+    TileSmem sm = tile_smem(max_local, tile_vertices);
+    const int4 h0 = tile_accumulate(V, S.pos, tile0 + blockIdx.x, sm);
+    for (int k = threadIdx.x; k < h0.y; k += blockDim.x) {
+        Block<float> acc;
+        acc.f[0] = sm.a(0, k);
+        acc.f[1] = sm.a(1, k);
+        acc.f[2] = sm.a(2, k);
+#pragma unroll
+        for (int j = 0; j < 6; ++j) acc.h[j] = sm.a(3 + j, k);
+        solve_and_update(S, h0.x + k, acc, invdt2, fb2);
+    }
+}
+
+// Block-wide FP64 sum into *out (one atomic per block).
+__device__ __forceinline__ void block_sum_atomic(double v, double *out)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ double part[32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) part[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (blockDim.x + 31) / 32; ++k) s += part[k];
+        atomicAdd(out, s);
+    }
+}
+
+// Residual with the tile layout: every tile of every colour (positions are not modified).
+__global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileView V, const DevState S,
+                                                                     int max_local, int tile_vertices, float invdt2,
+                                                                     double *out)
+{
+    TileSmem sm = tile_smem(max_local, tile_vertices);
+    const int4 h0 = tile_accumulate(V, S.pos, blockIdx.x, sm);
+    double r2 = 0.0;
+    for (int k = threadIdx.x; k < h0.y; k += blockDim.x) {
+        const float4 tg = S.tgt[h0.x + k];
+        const float4 d = sm.delta[k];
+        const double c = double(tg.w) * invdt2;
+        const double rx = c * (double(d.x) - tg.x) - sm.a(0, k);
+        const double ry = c * (double(d.y) - tg.y) - sm.a(1, k);
+        const double rz = c * (double(d.z) - tg.z) - sm.a(2, k);
+        r2 += rx * rx + ry * ry + rz * rz;
+    }
+    block_sum_atomic(r2, out);
+}
+
 // ||M/h^2 (x - y) + grad E(x)||^2 with per-vertex FP32 forces and an FP64 reduction.
 template <int G>
 __global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const DevState S, int nv, float invdt2,
@@ -138,16 +191,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const 
         const double rz = c * (double(ds.z) - tg.z) - acc.f[2];
         r2 = rx * rx + ry * ry + rz * rz;
     }
-    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
-    __shared__ double part[8];
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) part[w] = r2;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int k = 0; k < (blockDim.x + 31) / 32; ++k) s += part[k];
-        atomicAdd(out, s);
-    }
+    block_sum_atomic(r2, out);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -157,6 +201,14 @@ static int ceil_div(long long a, long long b) { return static_cast<int>((a + b -
 
 static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
 {
+    if (s.kernel == 2) {
+        const int t0 = s.TL.color_tiles[c], t1 = s.TL.color_tiles[c + 1];
+        if (t1 <= t0) return;
+        vbd_tile_kernel<<<t1 - t0, s.block, s.tile_smem, st>>>(
+            s.TV, s.S, t0, s.TL.max_local, s.TL.tile_vertices, static_cast<float>(1.0 / (s.h_sub * s.h_sub)),
+            static_cast<float>(s.P.fallback_condition * s.P.fallback_condition));
+        return;
+    }
     const int cs = s.L.color_start[c], ce = s.L.color_start[c + 1];
     if (ce <= cs) return;
     const int grid = ceil_div(static_cast<long long>(ce - cs) * s.lanes, s.block);
@@ -185,9 +237,16 @@ static void launch_end(const VbdSolver &s, cudaStream_t st) { launch_end_substep
 static void launch_residual(const VbdSolver &s, cudaStream_t st)
 {
     if (s.L.nv == 0) return;
-    const int grid = ceil_div(static_cast<long long>(s.L.nv) * s.lanes, s.block);
     const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
     double *out = s.d_resid.as<double>();
+    if (s.kernel == 2) {
+        const int nt = s.TL.color_tiles.back();
+        if (nt > 0)
+            residual_tile_kernel<<<nt, s.block, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, s.TL.tile_vertices,
+                                                                   invdt2, out);
+        return;
+    }
+    const int grid = ceil_div(static_cast<long long>(s.L.nv) * s.lanes, s.block);
     switch (s.lanes) {
     case 1: residual_kernel<1><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
     case 2: residual_kernel<2><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
@@ -277,7 +336,43 @@ spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params 
     S.adj = d_adj.as<int>();
     S.counters = d_counters.as<int>();
     S.status = reinterpret_cast<unsigned int *>(d_counters.as<int>() + 2);
+    SPGX_TRY_STATUS(setup_tiles());
     SPGX_TRY_STATUS(configure_launch());
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::setup_tiles()
+{
+    std::string err;
+    const int tv = P.tile_vertices ? P.tile_vertices : 64;
+    const spgx_status st = build_tiles(L, tv, TL, err);
+    if (st != SPGX_OK) {
+        set_error(err);
+        return st;
+    }
+    SPGX_TRY_STATUS(tb_hdr.upload(TL.hdr));
+    SPGX_TRY_STATUS(tb_halo.upload(TL.halo));
+    SPGX_TRY_STATUS(tb_anchor.upload(TL.rec_anchor));
+    SPGX_TRY_STATUS(tb_spring.upload(TL.rec_spring));
+    SPGX_TRY_STATUS(tb_flap.upload(TL.rec_flap));
+    SPGX_TRY_STATUS(tb_hinge.upload(TL.rec_hinge));
+    SPGX_TRY_STATUS(tb_stvk.upload(TL.rec_stvk));
+    SPGX_TRY_STATUS(tb_snh.upload(TL.rec_snh));
+    TV.hdr = tb_hdr.as<int4>();
+    TV.halo = tb_halo.as<int>();
+    TV.rec_anchor = tb_anchor.as<int4>();
+    TV.rec_spring = tb_spring.as<int4>();
+    TV.rec_flap = tb_flap.as<int4>();
+    TV.rec_hinge = tb_hinge.as<int4>();
+    TV.rec_stvk = tb_stvk.as<int4>();
+    TV.rec_snh = tb_snh.as<int4>();
+    tile_smem = tile_smem_bytes(std::max(1, TL.max_local), TL.tile_vertices);
+    if (tile_smem > 48 * 1024) {
+        SPGX_CUDA(cudaFuncSetAttribute(vbd_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(tile_smem)));
+        SPGX_CUDA(cudaFuncSetAttribute(residual_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(tile_smem)));
+    }
     return SPGX_OK;
 }
 
@@ -293,6 +388,10 @@ spgx_status VbdSolver::check_params(const spgx_vbd_params *p)
         set_error("lanes_per_vertex must be 0, 1, 2, 4, 8, 16 or 32");
         return SPGX_ERR_INVALID_ARG;
     }
+    if (p->kernel < 0 || p->kernel > 2 || p->tile_vertices < 0 || p->tile_vertices > kTileMaxVerts) {
+        set_error("kernel must be 0, 1 or 2 and tile_vertices in [0, 128]");
+        return SPGX_ERR_INVALID_ARG;
+    }
     if (p->block_size != 0 && (p->block_size % 32 != 0 || p->block_size < 32 || p->block_size > 256)) {
         set_error("block_size must be 0 or a multiple of 32 in [32, 256]");
         return SPGX_ERR_INVALID_ARG;
@@ -304,7 +403,11 @@ spgx_status VbdSolver::set_params(const spgx_vbd_params *params)
 {
     SPGX_TRY_STATUS(check_params(params));
     const bool relaunch = params->lanes_per_vertex != P.lanes_per_vertex || params->block_size != P.block_size ||
-                          params->device != P.device;
+                          params->kernel != P.kernel;
+    if (params->tile_vertices != P.tile_vertices) {
+        set_error("tile_vertices is fixed when the solver is created");
+        return SPGX_ERR_INVALID_ARG;
+    }
     if (params->device != P.device) {
         set_error("the device of a solver cannot change");
         return SPGX_ERR_INVALID_ARG;
@@ -316,57 +419,72 @@ spgx_status VbdSolver::set_params(const spgx_vbd_params *params)
     return SPGX_OK;
 }
 
-// Picks lanes-per-vertex and block size. Explicit parameters win; otherwise every candidate
-// (lanes up to twice the mean vertex degree, blocks 64/128/256) is timed on two colour sweeps
-// of this scene and the fastest kept. The state is restored afterwards.
+// Picks the kernel and its launch shape. Explicit parameters win; otherwise every candidate
+// (the lanes kernel with lanes up to twice the mean vertex degree and blocks 64/128/256, and
+// the tile kernel with 64/128/256 threads) is timed on two colour sweeps of this scene and the
+// fastest kept. The positions are restored afterwards.
 spgx_status VbdSolver::configure_launch()
 {
     graph_valid = false;
-    std::vector<int> lane_opts, block_opts;
-    if (P.lanes_per_vertex) {
-        lane_opts.push_back(P.lanes_per_vertex);
-    } else {
-        for (int g : {1, 2, 4, 8, 16, 32})
-            if (g == 1 || g <= 2 * std::max(1.0, L.mean_degree)) lane_opts.push_back(g);
-    }
+    struct Cand {
+        int kernel, lanes, block;
+    };
+    std::vector<Cand> cands;
+    const bool want_lanes = P.kernel == 0 || P.kernel == 1;
+    const bool want_tiles = P.kernel == 0 || P.kernel == 2;
+    std::vector<int> blocks;
     if (P.block_size)
-        block_opts.push_back(P.block_size);
+        blocks.push_back(P.block_size);
     else
-        block_opts = {64, 128, 256};
-    if (lane_opts.size() * block_opts.size() == 1 || L.nv == 0) {
-        lanes = lane_opts[0];
-        block = block_opts[0];
+        blocks = {64, 128, 256};
+    if (want_lanes) {
+        std::vector<int> lane_opts;
+        if (P.lanes_per_vertex)
+            lane_opts.push_back(P.lanes_per_vertex);
+        else
+            for (int g : {1, 2, 4, 8, 16, 32})
+                if (g == 1 || g <= 2 * std::max(1.0, L.mean_degree)) lane_opts.push_back(g);
+        for (int g : lane_opts)
+            for (int b : blocks) cands.push_back({1, g, b});
+    }
+    if (want_tiles)
+        for (int b : blocks)
+            if (b <= kTileThreads * 2) cands.push_back({2, TL.tile_vertices, b});
+    if (cands.size() == 1 || L.nv == 0) {
+        kernel = cands[0].kernel;
+        lanes = cands[0].lanes;
+        block = cands[0].block;
         return SPGX_OK;
     }
     SPGX_TRY_STATUS(X.upload_if_dirty(stream));
     SPGX_CUDA(cudaMemcpyAsync(d_backup.as<void>(), S.pos, size_t(L.nv) * 2 * sizeof(float4),
                               cudaMemcpyDeviceToDevice, stream));
     float best = 1e30f;
-    int bl = lane_opts[0], bb = block_opts[0];
-    for (int g : lane_opts)
-        for (int b : block_opts) {
-            lanes = g;
-            block = b;
-            launch_iterations(*this, 1, stream);
-            SPGX_CUDA(cudaEventRecord(ev0, stream));
-            launch_iterations(*this, 2, stream);
-            SPGX_CUDA(cudaEventRecord(ev1, stream));
-            SPGX_CUDA(cudaEventSynchronize(ev1));
-            float ms = 0.f;
-            SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-            if (ms < best) {
-                best = ms;
-                bl = g;
-                bb = b;
-            }
-            SPGX_CUDA(cudaMemcpyAsync(S.pos, d_backup.as<void>(), size_t(L.nv) * 2 * sizeof(float4),
-                                      cudaMemcpyDeviceToDevice, stream));
+    Cand pick = cands[0];
+    for (const auto &c : cands) {
+        kernel = c.kernel;
+        lanes = c.lanes;
+        block = c.block;
+        launch_iterations(*this, 1, stream);
+        SPGX_CUDA(cudaEventRecord(ev0, stream));
+        launch_iterations(*this, 2, stream);
+        SPGX_CUDA(cudaEventRecord(ev1, stream));
+        SPGX_CUDA(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        if (ms < best) {
+            best = ms;
+            pick = c;
         }
+        SPGX_CUDA(cudaMemcpyAsync(S.pos, d_backup.as<void>(), size_t(L.nv) * 2 * sizeof(float4),
+                                  cudaMemcpyDeviceToDevice, stream));
+    }
     SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, 4 * sizeof(int), stream));
     SPGX_CUDA(cudaStreamSynchronize(stream));
     SPGX_CUDA(cudaGetLastError());
-    lanes = bl;
-    block = bb;
+    kernel = pick.kernel;
+    lanes = pick.lanes;
+    block = pick.block;
     return SPGX_OK;
 }
 
@@ -654,13 +772,14 @@ spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts,
     SPGX_GUARD_END
 }
 
-spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *lanes_per_vertex, int32_t *block_size)
+spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *kernel, int32_t *lanes_per_vertex, int32_t *block_size)
 {
     SPGX_GUARD_BEGIN
     if (!h) {
         spgx::set_error("NULL solver handle");
         return SPGX_ERR_INVALID_ARG;
     }
+    if (kernel) *kernel = h->s->kernel;
     if (lanes_per_vertex) *lanes_per_vertex = h->s->lanes;
     if (block_size) *block_size = h->s->block;
     return SPGX_OK;

@@ -7,6 +7,7 @@
 #include "device_common.cuh"
 #include "layout.h"
 #include "state.h"
+#include "vbd_tile.cuh"
 
 namespace spgx {
 
@@ -22,6 +23,7 @@ struct VbdSolver {
     spgx_vbd_params P{};
     double h_sub{0.01};
     int device{0};
+    int kernel{1};  // 1: lanes-per-vertex kernel, 2: shared-memory tile kernel
     int lanes{1};
     int block{128};
     cudaStream_t stream{nullptr};
@@ -35,6 +37,10 @@ struct VbdSolver {
     HostBuf h_counters;
     DevTables T{};
     DevState S{};
+    TileLayout TL;
+    DevBuf tb_hdr, tb_halo, tb_anchor, tb_spring, tb_flap, tb_hinge, tb_stvk, tb_snh;
+    TileView TV{};
+    size_t tile_smem{0};
 
     VbdSolver() = default;
     VbdSolver(const VbdSolver &) = delete;
@@ -45,6 +51,7 @@ struct VbdSolver {
     static spgx_status check_params(const spgx_vbd_params *p);
     spgx_status set_params(const spgx_vbd_params *params);
     spgx_status configure_launch();
+    spgx_status setup_tiles();
     spgx_status build_graph();
     spgx_status residual_norm(double *out);
     spgx_status profile_sweeps(int iterations, double *color_ms);

@@ -18,8 +18,9 @@
 
 namespace spgx {
 
-// Work item: (type << 29) | element index in the type's table.
-constexpr int kItemShift = 29;
+// Work item: (type << 28) | element index in the type's table (types 1..5 keep the item
+// non-negative; tables are limited to 2^28 elements).
+constexpr int kItemShift = 28;
 constexpr int kItemMask = (1 << kItemShift) - 1;
 
 __device__ __forceinline__ void add_delta(float4 *pos, int v, V3f dx)
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, floa
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int item = __ldg(items + t);
-    const int type = item >> kItemShift;
+    const int type = (item >> kItemShift) & 7;
     const int e = item & kItemMask;
     switch (type) {
     case SPGX_ENERGY_SPRING: {
@@ -254,6 +255,12 @@ struct XpbdSolver {
         SPGX_TRY_STATUS(X.init(L));
         SPGX_TRY_STATUS(EB.upload(L.el, T));
         SPGX_TRY_STATUS(d_anchor_v.upload(L.el.anchor_v));
+        const size_t cap = size_t(1) << kItemShift;
+        if (L.el.anchors.size() >= cap || L.el.springs.size() >= cap || L.el.bend_idx.size() >= cap ||
+            L.el.stvk_idx.size() >= cap || L.el.snh_idx.size() >= cap) {
+            set_error("XPBD supports at most 2^28 stencils per energy type");
+            return SPGX_ERR_INVALID_ARG;
+        }
         // Phases: energy slot k, colour c (xpbd.cpp:84-95), over all objects at once. Anchors
         // run in their own phases so the generic kernel never branches to them.
         int max_e = 0;

@@ -47,7 +47,7 @@ class VbdParams(C.Structure):
                 ("gravity", C.c_double * 3), ("tolerance", C.c_double), ("max_iterations", C.c_int32),
                 ("check_interval", C.c_int32), ("fallback_condition", C.c_double),
                 ("lanes_per_vertex", C.c_int32), ("block_size", C.c_int32), ("use_graph", C.c_int32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("kernel", C.c_int32), ("tile_vertices", C.c_int32)]
 
 
 class XpbdParams(C.Structure):
@@ -91,7 +91,7 @@ def lib():
         L.spgx_vbd_num_colors.argtypes = [vp, i32, ip]
         L.spgx_vbd_get_colors.argtypes = [vp, i32, ip]
         L.spgx_vbd_get_adjacency.argtypes = [vp, i32, ip, ip, C.POINTER(C.c_int64)]
-        L.spgx_vbd_get_launch.argtypes = [vp, ip, ip]
+        L.spgx_vbd_get_launch.argtypes = [vp, ip, ip, ip]
         L.spgx_vbd_profile_sweeps.argtypes = [vp, i32, dp]
         L.spgx_eval_vertex_blocks.argtypes = [i32, i32, dp, dp, ip, dp, dp]
         L.spgx_eval_constraints.argtypes = [i32, i32, dp, dp, dp, dp]
@@ -147,7 +147,7 @@ class Descriptor:
 
 def vbd_params(dt=0.01, substeps=1, iterations=1, gravity=(0.0, -9.8, 0.0), tolerance=0.0, max_iterations=1000,
                check_interval=10, fallback_condition=1e6, lanes_per_vertex=0, block_size=0, use_graph=1,
-               device=0) -> VbdParams:
+               device=0, kernel=0, tile_vertices=64) -> VbdParams:
     p = VbdParams()
     lib().spgx_vbd_params_default(C.byref(p))
     p.dt, p.substeps, p.iterations = dt, substeps, iterations
@@ -155,6 +155,7 @@ def vbd_params(dt=0.01, substeps=1, iterations=1, gravity=(0.0, -9.8, 0.0), tole
     p.tolerance, p.max_iterations, p.check_interval = tolerance, max_iterations, check_interval
     p.fallback_condition = fallback_condition
     p.lanes_per_vertex, p.block_size, p.use_graph, p.device = lanes_per_vertex, block_size, use_graph, device
+    p.kernel, p.tile_vertices = kernel, tile_vertices
     return p
 
 
@@ -240,9 +241,10 @@ class VbdSolver:
         return out
 
     def launch(self):
-        g, b = C.c_int32(), C.c_int32()
-        check(lib().spgx_vbd_get_launch(self.h, C.byref(g), C.byref(b)))
-        return g.value, b.value
+        """(kernel, lanes_per_vertex or tile vertices, block size) chosen by the solver."""
+        k, g, b = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().spgx_vbd_get_launch(self.h, C.byref(k), C.byref(g), C.byref(b)))
+        return k.value, g.value, b.value
 
 
 class XpbdSolver:
