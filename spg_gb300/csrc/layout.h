@@ -84,27 +84,25 @@ struct SceneLayout {
 };
 
 // Tiles of one colour for the shared-memory VBD kernel. A tile is a run of consecutive
-// same-colour vertices (internal order) plus the halo of other vertices its incidences read;
-// its incidences are stored as self-contained records with tile-local vertex indices and
-// inline parameters, class by class, each class in vertex-interleaved order (record r of a
-// class belongs to a different vertex than record r + 1 whenever the tile has several).
+// same-colour vertices (internal order) plus the halo of other vertices its incidences read.
+// Its incidences are stored as one contiguous block of self-contained records (tile-local
+// vertex indices, inline parameters): vertex by vertex in tile order, per vertex class by
+// class as in the per-vertex header counts, reference order inside a class. Record sizes in
+// 16-byte units: anchor 1, spring 1, flap 1, hinge 1, StVK 3, SNH 4.
 constexpr int kTileMaxLocal = 1024;  // tile vertices + halo vertices
 constexpr int kTileMaxVerts = 128;
+constexpr int kTileMaxRecords = 4096;  // 16-byte record units per tile
 
 struct TileLayout {
     int tile_vertices{0};
     int max_local{0};
+    int max_records{0};
     std::vector<int32_t> color_tiles;  // n_colors + 1: tile index range of each colour
-    // Per tile, 4 x I4: {vstart, nvt, halo_off, n_halo}, {off anchor, spring, flap, hinge},
-    // {off stvk, snh, n anchor, n spring}, {n flap, n hinge, n stvk, n snh}.
+    // Per tile: {vstart, nvt, halo_off, n_halo}, {rec_off, n_rec, 0, 0} (16-byte units).
     std::vector<I4> hdr;
     std::vector<int32_t> halo;
-    std::vector<I4> rec_anchor;  // 2 per record
-    std::vector<I4> rec_spring;  // 1
-    std::vector<I4> rec_flap;    // 1
-    std::vector<I4> rec_hinge;   // 1
-    std::vector<I4> rec_stvk;    // 3
-    std::vector<I4> rec_snh;     // 4
+    std::vector<I4> records;
+    std::vector<int32_t> vrec;  // per internal vertex: record offset inside its tile's block
 };
 
 spgx_status build_tiles(const SceneLayout &L, int tile_vertices, TileLayout &out, std::string &err);

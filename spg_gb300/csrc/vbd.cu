@@ -26,11 +26,10 @@ namespace spgx {
 // H = m/h^2 I + sum of blocks, f = -m/h^2 (x - y) + sum of forces, x += H^-1 f when
 // det(H) > 1e-10. The solve runs in FP32 on the max-norm-scaled block unless its Frobenius
 // condition estimate exceeds the fallback threshold, in which case it is redone in FP64.
-__device__ __forceinline__ void solve_and_update(const DevState &S, int v, const Block<float> &acc, float invdt2,
-                                                 float fb2)
+__device__ __forceinline__ void solve_and_update(const DevState &S, int v, const Block<float> &acc, float4 d4,
+                                                 float invdt2, float fb2)
 {
     const float4 tg = S.tgt[v];
-    const float4 d4 = S.pos[2 * v + 1];
     const float c = tg.w * invdt2;
     const float f0 = acc.f[0] - c * (d4.x - tg.x);
     const float f1 = acc.f[1] - c * (d4.y - tg.y);
@@ -106,25 +105,37 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
     block_zero(acc);
     accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
     group_reduce<G>(acc);
-    if (active && lane == 0) solve_and_update(S, v, acc, invdt2, fb2);
+    if (active && lane == 0) solve_and_update(S, v, acc, S.pos[2 * v + 1], invdt2, fb2);
 }
 
-// One colour phase with the shared-memory tile kernel: one CTA per tile of the colour.
+// One colour phase with the shared-memory tile kernel: one CTA per tile of the colour,
+// G lanes per tile vertex (blockDim = tile_vertices * G).
+template <int G>
 __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V, const DevState S, int tile0,
-                                                                int max_local, int tile_vertices, float invdt2,
-                                                                float fb2)
+                                                                int max_local, float invdt2, float fb2)
 {
-    TileSmem sm = tile_smem(max_local, tile_vertices);
-    const int4 h0 = tile_accumulate(V, S.pos, tile0 + blockIdx.x, sm);
-    for (int k = threadIdx.x; k < h0.y; k += blockDim.x) {
-        Block<float> acc;
-        acc.f[0] = sm.a(0, k);
-        acc.f[1] = sm.a(1, k);
-        acc.f[2] = sm.a(2, k);
-#pragma unroll
-        for (int j = 0; j < 6; ++j) acc.h[j] = sm.a(3 + j, k);
-        solve_and_update(S, h0.x + k, acc, invdt2, fb2);
+    extern __shared__ float4 dyn[];
+    float4 *sb = dyn;
+    float4 *sd = dyn + max_local;
+    int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
+    const int4 h0 = tile_stage(V, S.pos, tile0 + blockIdx.x, sb, sd, srec);
+    const int lv = threadIdx.x / G;
+    const int lane = threadIdx.x & (G - 1);
+    const bool active = lv < h0.y;
+    int4 hv = make_int4(0, 0, 0, 0);
+    int roff = 0;
+    TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
+    if (active) {
+        hv = __ldg(S.hdr + h0.x + lv);
+        roff = __ldg(V.vrec + h0.x + lv);
+        cx.bs = v3(sb[lv]);
+        cx.ds = v3(sd[lv]);
     }
+    Block<float> acc;
+    block_zero(acc);
+    tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+    group_reduce<G>(acc);
+    if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], invdt2, fb2);
 }
 
 // Block-wide FP64 sum into *out (one atomic per block).
@@ -143,21 +154,39 @@ __device__ __forceinline__ void block_sum_atomic(double v, double *out)
 }
 
 // Residual with the tile layout: every tile of every colour (positions are not modified).
+template <int G>
 __global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileView V, const DevState S,
-                                                                     int max_local, int tile_vertices, float invdt2,
-                                                                     double *out)
+                                                                     int max_local, float invdt2, double *out)
 {
-    TileSmem sm = tile_smem(max_local, tile_vertices);
-    const int4 h0 = tile_accumulate(V, S.pos, blockIdx.x, sm);
+    extern __shared__ float4 dyn[];
+    float4 *sb = dyn;
+    float4 *sd = dyn + max_local;
+    int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
+    const int4 h0 = tile_stage(V, S.pos, blockIdx.x, sb, sd, srec);
+    const int lv = threadIdx.x / G;
+    const int lane = threadIdx.x & (G - 1);
+    const bool active = lv < h0.y;
+    int4 hv = make_int4(0, 0, 0, 0);
+    int roff = 0;
+    TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
+    if (active) {
+        hv = __ldg(S.hdr + h0.x + lv);
+        roff = __ldg(V.vrec + h0.x + lv);
+        cx.bs = v3(sb[lv]);
+        cx.ds = v3(sd[lv]);
+    }
+    Block<float> acc;
+    block_zero(acc);
+    tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+    group_reduce<G>(acc);
     double r2 = 0.0;
-    for (int k = threadIdx.x; k < h0.y; k += blockDim.x) {
-        const float4 tg = S.tgt[h0.x + k];
-        const float4 d = sm.delta[k];
+    if (active && lane == 0) {
+        const float4 tg = S.tgt[h0.x + lv];
         const double c = double(tg.w) * invdt2;
-        const double rx = c * (double(d.x) - tg.x) - sm.a(0, k);
-        const double ry = c * (double(d.y) - tg.y) - sm.a(1, k);
-        const double rz = c * (double(d.z) - tg.z) - sm.a(2, k);
-        r2 += rx * rx + ry * ry + rz * rz;
+        const double rx = c * (double(cx.ds.x) - tg.x) - acc.f[0];
+        const double ry = c * (double(cx.ds.y) - tg.y) - acc.f[1];
+        const double rz = c * (double(cx.ds.z) - tg.z) - acc.f[2];
+        r2 = rx * rx + ry * ry + rz * rz;
     }
     block_sum_atomic(r2, out);
 }
@@ -204,9 +233,15 @@ static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
     if (s.kernel == 2) {
         const int t0 = s.TL.color_tiles[c], t1 = s.TL.color_tiles[c + 1];
         if (t1 <= t0) return;
-        vbd_tile_kernel<<<t1 - t0, s.block, s.tile_smem, st>>>(
-            s.TV, s.S, t0, s.TL.max_local, s.TL.tile_vertices, static_cast<float>(1.0 / (s.h_sub * s.h_sub)),
-            static_cast<float>(s.P.fallback_condition * s.P.fallback_condition));
+        const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
+        const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
+        const int threads = s.TL.tile_vertices * s.lanes;
+        switch (s.lanes) {
+        case 1: vbd_tile_kernel<1><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        case 2: vbd_tile_kernel<2><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        case 4: vbd_tile_kernel<4><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        default: vbd_tile_kernel<8><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        }
         return;
     }
     const int cs = s.L.color_start[c], ce = s.L.color_start[c + 1];
@@ -241,9 +276,15 @@ static void launch_residual(const VbdSolver &s, cudaStream_t st)
     double *out = s.d_resid.as<double>();
     if (s.kernel == 2) {
         const int nt = s.TL.color_tiles.back();
-        if (nt > 0)
-            residual_tile_kernel<<<nt, s.block, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, s.TL.tile_vertices,
-                                                                   invdt2, out);
+        const int threads = s.TL.tile_vertices * s.lanes;
+        if (nt > 0) {
+            switch (s.lanes) {
+            case 1: residual_tile_kernel<1><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+            case 2: residual_tile_kernel<2><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+            case 4: residual_tile_kernel<4><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+            default: residual_tile_kernel<8><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+            }
+        }
         return;
     }
     const int grid = ceil_div(static_cast<long long>(s.L.nv) * s.lanes, s.block);
@@ -352,26 +393,25 @@ spgx_status VbdSolver::setup_tiles()
     }
     SPGX_TRY_STATUS(tb_hdr.upload(TL.hdr));
     SPGX_TRY_STATUS(tb_halo.upload(TL.halo));
-    SPGX_TRY_STATUS(tb_anchor.upload(TL.rec_anchor));
-    SPGX_TRY_STATUS(tb_spring.upload(TL.rec_spring));
-    SPGX_TRY_STATUS(tb_flap.upload(TL.rec_flap));
-    SPGX_TRY_STATUS(tb_hinge.upload(TL.rec_hinge));
-    SPGX_TRY_STATUS(tb_stvk.upload(TL.rec_stvk));
-    SPGX_TRY_STATUS(tb_snh.upload(TL.rec_snh));
+    SPGX_TRY_STATUS(tb_records.upload(TL.records));
+    SPGX_TRY_STATUS(tb_vrec.upload(TL.vrec));
     TV.hdr = tb_hdr.as<int4>();
     TV.halo = tb_halo.as<int>();
-    TV.rec_anchor = tb_anchor.as<int4>();
-    TV.rec_spring = tb_spring.as<int4>();
-    TV.rec_flap = tb_flap.as<int4>();
-    TV.rec_hinge = tb_hinge.as<int4>();
-    TV.rec_stvk = tb_stvk.as<int4>();
-    TV.rec_snh = tb_snh.as<int4>();
-    tile_smem = tile_smem_bytes(std::max(1, TL.max_local), TL.tile_vertices);
+    TV.records = tb_records.as<int4>();
+    TV.vrec = tb_vrec.as<int>();
+    tile_smem = tile_smem_bytes(std::max(1, TL.max_local), std::max(1, TL.max_records));
     if (tile_smem > 48 * 1024) {
-        SPGX_CUDA(cudaFuncSetAttribute(vbd_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(tile_smem)));
-        SPGX_CUDA(cudaFuncSetAttribute(residual_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(tile_smem)));
+        auto raise = [this](const void *fn) -> cudaError_t {
+            return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tile_smem));
+        };
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<1>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<2>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<4>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<8>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<1>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<2>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<4>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<8>)));
     }
     return SPGX_OK;
 }
@@ -448,8 +488,9 @@ spgx_status VbdSolver::configure_launch()
             for (int b : blocks) cands.push_back({1, g, b});
     }
     if (want_tiles)
-        for (int b : blocks)
-            if (b <= kTileThreads * 2) cands.push_back({2, TL.tile_vertices, b});
+        for (int g : {1, 2, 4, 8})
+            if (TL.tile_vertices * g <= kTileThreads && (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
+                cands.push_back({2, g, TL.tile_vertices * g});
     if (cands.size() == 1 || L.nv == 0) {
         kernel = cands[0].kernel;
         lanes = cands[0].lanes;

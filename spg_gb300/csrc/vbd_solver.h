@@ -38,7 +38,7 @@ struct VbdSolver {
     DevTables T{};
     DevState S{};
     TileLayout TL;
-    DevBuf tb_hdr, tb_halo, tb_anchor, tb_spring, tb_flap, tb_hinge, tb_stvk, tb_snh;
+    DevBuf tb_hdr, tb_halo, tb_records, tb_vrec;
     TileView TV{};
     size_t tile_smem{0};
 
