@@ -197,6 +197,19 @@ spgx_status spgx_vbd_profile_sweeps(spgx_vbd *h, int32_t iterations, double *col
  * grad = n * 3 (energy gradient segment of the slot), hess = n * 9 (row-major 3x3 block). */
 spgx_status spgx_eval_vertex_blocks(int32_t type, int32_t n, const double *X, const double *params,
                                     const int32_t *slots, double *grad, double *hess);
+/* Allocation-free variant of spgx_eval_vertex_blocks, for callers that cannot allocate device
+ * memory: hosts whose device memory is owned by another allocator (a framework's memory pool
+ * that leaves nothing to cudaMalloc), or code paths that must not add allocation latency
+ * or fragmentation after start-up. It calls no cudaMalloc, cudaFree or other allocating
+ * routine: inputs and outputs are the caller's host arrays, and the device staging is one
+ * fixed array inside the library (about 750 KB, held by every GPU that loads the library
+ * until the process exits). Capacity: n <= 4096 incidences per call; larger n returns
+ * SPGX_ERR_INVALID_ARG. The first call on a device looks up that array's device address
+ * (once per device), so make that first call before any stream capture. All calls share the
+ * array: calls that overlap on the same GPU race. Results equal spgx_eval_vertex_blocks'.
+ * No counterpart in the reference. */
+spgx_status spgx_eval_vertex_blocks_noalloc(int32_t type, int32_t n, const double *X, const double *params,
+                                            const int32_t *slots, double *grad, double *hess);
 /* Constraint values (n * nc) and gradients (n * nc * 3 * stencil_size, constraint-major)
  * as used by the XPBD projection. */
 spgx_status spgx_eval_constraints(int32_t type, int32_t n, const double *X, const double *params, double *C,

@@ -2,6 +2,8 @@
 // per-element derivative parity checks (spgx_eval_vertex_blocks / spgx_eval_constraints).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "api_internal.h"
@@ -104,6 +106,73 @@ __global__ void eval_constraints_kernel(int type, int n, int S, int P, int NC, c
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant of the element evaluation. Its device staging lives in one
+// file-scope array that every GPU loading this library holds (about 750 KB) until the process
+// exits; every call shares it, so calls that overlap on a GPU race on it.
+constexpr int kNoAllocMaxIncidences = 4096;
+constexpr int kNoAllocMaxStencil = 4;
+constexpr int kNoAllocMaxParams = 22;
+
+struct NoAllocScratch {
+    float X[kNoAllocMaxIncidences * kNoAllocMaxStencil * 3];
+    float params[kNoAllocMaxIncidences * kNoAllocMaxParams];
+    int slots[kNoAllocMaxIncidences];
+    float grad[kNoAllocMaxIncidences * 3];
+    float hess[kNoAllocMaxIncidences * 9];
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of the scratch array on the current device, looked up once per device with
+// that device current (the host-side symbol is only a stand-in, never a device address).
+static spgx_status noalloc_scratch(NoAllocScratch **out)
+{
+    static std::mutex mutex;
+    static NoAllocScratch *addr[256] = {};
+    int dev = 0;
+    SPGX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) {
+        set_error("device ordinal out of range");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(mutex);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+            return SPGX_ERR_CUDA;
+        }
+        addr[dev] = static_cast<NoAllocScratch *>(p);
+    }
+    *out = addr[dev];
+    return SPGX_OK;
+}
+
+// Converts count doubles to floats through a stack buffer and copies them to dst.
+static spgx_status upload_floats(float *dst, const double *src, size_t count)
+{
+    float buf[1024];
+    for (size_t o = 0; o < count; o += 1024) {
+        const size_t m = std::min<size_t>(1024, count - o);
+        for (size_t k = 0; k < m; ++k) buf[k] = static_cast<float>(src[o + k]);
+        SPGX_CUDA(cudaMemcpy(dst + o, buf, m * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return SPGX_OK;
+}
+
+static spgx_status download_floats(double *dst, const float *src, size_t count)
+{
+    float buf[1024];
+    for (size_t o = 0; o < count; o += 1024) {
+        const size_t m = std::min<size_t>(1024, count - o);
+        SPGX_CUDA(cudaMemcpy(buf, src + o, m * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < m; ++k) dst[o + k] = buf[k];
+    }
+    return SPGX_OK;
+}
+
 }  // namespace spgx
 
 extern "C" {
@@ -148,6 +217,47 @@ spgx_status spgx_eval_vertex_blocks(int32_t type, int32_t n, const double *X, co
     SPGX_CUDA(cudaMemcpy(hh.data(), dH.as<float>(), hh.size() * sizeof(float), cudaMemcpyDeviceToHost));
     for (size_t k = 0; k < g.size(); ++k) grad[k] = g[k];
     for (size_t k = 0; k < hh.size(); ++k) hess[k] = hh[k];
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_eval_vertex_blocks_noalloc(int32_t type, int32_t n, const double *X, const double *params,
+                                            const int32_t *slots, double *grad, double *hess)
+{
+    SPGX_GUARD_BEGIN
+    const int S = spgx::stencil_size(type), P = spgx::param_count(type);
+    if (S == 0) {
+        spgx::set_error("unsupported energy type");
+        return SPGX_ERR_UNSUPPORTED_ENERGY;
+    }
+    if (n < 0 || (n > 0 && (!X || !params || !slots || !grad || !hess))) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (n > spgx::kNoAllocMaxIncidences) {
+        spgx::set_error("spgx_eval_vertex_blocks_noalloc: n = " + std::to_string(n) + " exceeds the fixed capacity of " +
+                        std::to_string(spgx::kNoAllocMaxIncidences) + " incidences per call");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (n == 0) return SPGX_OK;
+    for (int i = 0; i < n; ++i)
+        if (slots[i] < 0 || slots[i] >= S) {
+            spgx::set_error("slot out of range");
+            return SPGX_ERR_INVALID_ARG;
+        }
+    int dev = 0;
+    SPGX_CUDA(cudaGetDevice(&dev));
+    SPGX_TRY_STATUS(spgx::select_device(dev));
+    spgx::NoAllocScratch *sc = nullptr;
+    SPGX_TRY_STATUS(spgx::noalloc_scratch(&sc));
+    SPGX_TRY_STATUS(spgx::upload_floats(sc->X, X, size_t(n) * S * 3));
+    SPGX_TRY_STATUS(spgx::upload_floats(sc->params, params, size_t(n) * P));
+    SPGX_CUDA(cudaMemcpy(sc->slots, slots, size_t(n) * sizeof(int), cudaMemcpyHostToDevice));
+    spgx::eval_blocks_kernel<<<(n + 127) / 128, 128>>>(type, n, S, P, sc->X, sc->params, sc->slots, sc->grad,
+                                                       sc->hess);
+    SPGX_CUDA(cudaGetLastError());
+    SPGX_TRY_STATUS(spgx::download_floats(grad, sc->grad, size_t(n) * 3));
+    SPGX_TRY_STATUS(spgx::download_floats(hess, sc->hess, size_t(n) * 9));
     return SPGX_OK;
     SPGX_GUARD_END
 }

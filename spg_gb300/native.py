@@ -95,6 +95,7 @@ def lib():
         L.spgx_vbd_profile_sweeps.argtypes = [vp, i32, dp]
         L.spgx_eval_vertex_blocks.argtypes = [i32, i32, dp, dp, ip, dp, dp]
         L.spgx_eval_constraints.argtypes = [i32, i32, dp, dp, dp, dp]
+        L.spgx_eval_vertex_blocks_noalloc.argtypes = [i32, i32, dp, dp, ip, dp, dp]
         L.spgx_xpbd_create.argtypes = [C.POINTER(SceneDesc), C.POINTER(XpbdParams), C.POINTER(vp)]
         L.spgx_xpbd_destroy.argtypes = [vp]
         L.spgx_xpbd_set_params.argtypes = [vp, C.POINTER(XpbdParams)]
@@ -304,6 +305,20 @@ def eval_vertex_blocks(etype, X, params, slots):
     H = np.zeros((n, 9))
     check(lib().spgx_eval_vertex_blocks(etype, n, _p(X, C.c_double), _p(prm, C.c_double), _p(sl, C.c_int32),
                                         _p(g, C.c_double), _p(H, C.c_double)))
+    return g, H.reshape(n, 3, 3)
+
+
+def eval_vertex_blocks_noalloc(etype, X, params, slots):
+    """Same as eval_vertex_blocks through the allocation-free entry point (n <= 4096)."""
+    S, P = STENCIL_SIZE[etype], PARAM_COUNT[etype]
+    X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, S * 3)
+    n = X.shape[0]
+    prm = np.ascontiguousarray(params, dtype=np.float64).reshape(n, P)
+    sl = np.ascontiguousarray(slots, dtype=np.int32).reshape(n)
+    g = np.zeros((n, 3))
+    H = np.zeros((n, 9))
+    check(lib().spgx_eval_vertex_blocks_noalloc(etype, n, _p(X, C.c_double), _p(prm, C.c_double),
+                                                _p(sl, C.c_int32), _p(g, C.c_double), _p(H, C.c_double)))
     return g, H.reshape(n, 3, 3)
 
 
