@@ -52,11 +52,17 @@ def _dist():
     return dist, rank, local, ws
 
 
+def _device(local):
+    return "cpu" if local is None else f"cuda:{local}"
+
+
 def _barrier(dist, local):
+    """Barrier across ranks (local is the CUDA device, or None for CPU/gloo ranks)."""
     if dist is None:
         return
     import torch
-    torch.cuda.synchronize(local)
+    if local is not None:
+        torch.cuda.synchronize(local)
     dist.barrier()
 
 
@@ -64,7 +70,7 @@ def _max_over_ranks(dist, local, v: float) -> float:
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    t = torch.tensor([v], dtype=torch.float64, device=_device(local))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -73,7 +79,7 @@ def _sum_over_ranks(dist, local, v: float) -> float:
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    t = torch.tensor([v], dtype=torch.float64, device=_device(local))
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
