@@ -64,6 +64,14 @@ __device__ __forceinline__ V3f rel_pos(const float4 *__restrict__ pos, int j, V3
 
 __device__ __forceinline__ int warp_max(int v) { return __reduce_max_sync(0xffffffffu, v); }
 
+// Waits until the previous kernel on the stream has completed and its writes are visible
+// (programmatic dependent launch); a no-op when the kernel was launched without it.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+// Lets the next kernel on the stream start launching once every CTA of this grid has called it
+// or exited (the next kernel still waits in wait_prior_grid for this grid's completion).
+__device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+
 // Walks the vertex's class-sorted incidence list with G lanes per vertex (lane-strided) and
 // accumulates the force and Hessian block of every incident element into acc.
 // Loop trip counts are warp-uniform (max over the warp), so all 32 lanes stay converged.

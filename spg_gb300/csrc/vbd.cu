@@ -96,8 +96,9 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
     const bool active = v < cend;
     int4 h = make_int4(0, 0, 0, 0);
     V3f bs = mk(0.f, 0.f, 0.f), ds = bs;
+    if (active) h = __ldg(S.hdr + v);
+    wait_prior_grid();
     if (active) {
-        h = __ldg(S.hdr + v);
         bs = v3(__ldg(S.pos + 2 * v));
         ds = v3(__ldg(S.pos + 2 * v + 1));
     }
@@ -105,6 +106,7 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
     block_zero(acc);
     accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
     group_reduce<G>(acc);
+    allow_next_grid();
     if (active && lane == 0) solve_and_update(S, v, acc, S.pos[2 * v + 1], invdt2, fb2);
 }
 
@@ -135,6 +137,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
     block_zero(acc);
     tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
     group_reduce<G>(acc);
+    allow_next_grid();
     if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], invdt2, fb2);
 }
 
@@ -228,6 +231,25 @@ __global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const 
 
 static int ceil_div(long long a, long long b) { return static_cast<int>((a + b - 1) / b); }
 
+// Launches a tile kernel with programmatic dependent launch: its static prologue (tile header,
+// record copies, halo indices) overlaps the tail of the previous kernel, and it waits
+// (griddepcontrol.wait) before copying positions, which it reads through L2 only.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
 {
     if (s.kernel == 2) {
@@ -237,10 +259,10 @@ static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
         const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
         const int threads = s.TL.tile_vertices * s.lanes;
         switch (s.lanes) {
-        case 1: vbd_tile_kernel<1><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        case 2: vbd_tile_kernel<2><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        case 4: vbd_tile_kernel<4><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        default: vbd_tile_kernel<8><<<t1 - t0, threads, s.tile_smem, st>>>(s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        case 1: launch_pdl(vbd_tile_kernel<1>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        case 2: launch_pdl(vbd_tile_kernel<2>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        case 4: launch_pdl(vbd_tile_kernel<4>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+        default: launch_pdl(vbd_tile_kernel<8>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
         }
         return;
     }
@@ -249,6 +271,8 @@ static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
     const int grid = ceil_div(static_cast<long long>(ce - cs) * s.lanes, s.block);
     const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
     const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
+    // Launched without programmatic overlap: this kernel reads neighbour positions through the
+    // read-only data path, which must not run while the previous colour still writes them.
     switch (s.lanes) {
     case 1: vbd_color_kernel<1><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
     case 2: vbd_color_kernel<2><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;

@@ -53,8 +53,9 @@ struct TileCtx {
     }
 };
 
-// Stages the tile into shared memory. Returns {vstart, nvt, halo_off, n_halo}; the caller's
-// thread group owns vertex threadIdx.x / G of the tile.
+// Stages the tile into shared memory. The tile's records and halo indices never change, so
+// they are fetched before waiting for the previous colour; the positions after. Returns
+// {vstart, nvt, halo_off, n_halo}; thread group threadIdx.x / G owns that tile vertex.
 __device__ __forceinline__ int4 tile_stage(const TileView &V, const float4 *__restrict__ pos, int tile,
                                            float4 *sb, float4 *sd, int4 *srec)
 {
@@ -62,7 +63,23 @@ __device__ __forceinline__ int4 tile_stage(const TileView &V, const float4 *__re
     const int4 h1 = __ldg(V.hdr + 2 * tile + 1);
     for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
     const int nvt = h0.y, nl = h0.y + h0.w;
-    for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+    constexpr int kMaxHaloPerThread = 8;
+    int gidx[kMaxHaloPerThread];
+#pragma unroll
+    for (int k = 0; k < kMaxHaloPerThread; ++k) {
+        const int i = threadIdx.x + k * blockDim.x;
+        gidx[k] = i < nvt ? h0.x + i : (i < nl ? __ldg(V.halo + h0.z + i - nvt) : -1);
+    }
+    wait_prior_grid();
+#pragma unroll
+    for (int k = 0; k < kMaxHaloPerThread; ++k) {
+        const int i = threadIdx.x + k * blockDim.x;
+        if (gidx[k] >= 0) {
+            cp_async16(sb + i, pos + 2 * gidx[k]);
+            cp_async16(sd + i, pos + 2 * gidx[k] + 1);
+        }
+    }
+    for (int i = threadIdx.x + kMaxHaloPerThread * blockDim.x; i < nl; i += blockDim.x) {
         const int g = i < nvt ? h0.x + i : __ldg(V.halo + h0.z + i - nvt);
         cp_async16(sb + i, pos + 2 * g);
         cp_async16(sd + i, pos + 2 * g + 1);
@@ -93,40 +110,51 @@ __device__ __forceinline__ void tile_vertex_accumulate(const TileCtx &cx, int4 h
         }
         off += n;
     }
+    // Springs, bending flaps and bending hinges take two incidences per round so their
+    // arithmetic forms two independent dependency chains. A missing second incidence is
+    // replaced by a copy of the first with zero stiffness (its contribution is exactly 0).
     {  // springs: {other, L0, k}
         const int n = (h.y >> 16) & 0xffff;
-        const int rounds = warp_max((n + G - 1) / G);
+        const int rounds = warp_max((n + 2 * G - 1) / (2 * G));
         for (int r = 0; r < rounds; ++r) {
-            const int i = r * G + lane;
-            if (i < n) {
-                const int4 q = cx.rec[off + i];
-                spring_block(zero, cx.rel(q.x), __int_as_float(q.y), __int_as_float(q.z), acc);
+            const int i0 = 2 * r * G + lane, i1 = i0 + G;
+            if (i0 < n) {
+                const int4 q0 = cx.rec[off + i0];
+                const int4 q1 = cx.rec[off + (i1 < n ? i1 : i0)];
+                spring_block(zero, cx.rel(q0.x), __int_as_float(q0.y), __int_as_float(q0.z), acc);
+                spring_block(zero, cx.rel(q1.x), __int_as_float(q1.y), i1 < n ? __int_as_float(q1.z) : 0.f, acc);
             }
         }
         off += n;
     }
     {  // bending flaps: {p0 | p1 << 16, other flap, signed theta0, k}
         const int n = h.z & 0xffff;
-        const int rounds = warp_max((n + G - 1) / G);
+        const int rounds = warp_max((n + 2 * G - 1) / (2 * G));
         for (int r = 0; r < rounds; ++r) {
-            const int i = r * G + lane;
-            if (i < n) {
-                const int4 q = cx.rec[off + i];
-                bending_flap_block(cx.rel(q.x & 0xffff), cx.rel(q.x >> 16), zero, cx.rel(q.y), __int_as_float(q.z),
-                                   __int_as_float(q.w), acc);
+            const int i0 = 2 * r * G + lane, i1 = i0 + G;
+            if (i0 < n) {
+                const int4 q0 = cx.rec[off + i0];
+                const int4 q1 = cx.rec[off + (i1 < n ? i1 : i0)];
+                bending_flap_block(cx.rel(q0.x & 0xffff), cx.rel(q0.x >> 16), zero, cx.rel(q0.y), __int_as_float(q0.z),
+                                   __int_as_float(q0.w), acc);
+                bending_flap_block(cx.rel(q1.x & 0xffff), cx.rel(q1.x >> 16), zero, cx.rel(q1.y), __int_as_float(q1.z),
+                                   i1 < n ? __int_as_float(q1.w) : 0.f, acc);
             }
         }
         off += n;
     }
     {  // bending hinges: {other hinge, p2 | p3 << 16, signed theta0, k}
         const int n = (h.z >> 16) & 0xffff;
-        const int rounds = warp_max((n + G - 1) / G);
+        const int rounds = warp_max((n + 2 * G - 1) / (2 * G));
         for (int r = 0; r < rounds; ++r) {
-            const int i = r * G + lane;
-            if (i < n) {
-                const int4 q = cx.rec[off + i];
-                bending_hinge_block(cx.rel(q.x), zero, cx.rel(q.y & 0xffff), cx.rel(q.y >> 16), __int_as_float(q.z),
-                                    __int_as_float(q.w), acc);
+            const int i0 = 2 * r * G + lane, i1 = i0 + G;
+            if (i0 < n) {
+                const int4 q0 = cx.rec[off + i0];
+                const int4 q1 = cx.rec[off + (i1 < n ? i1 : i0)];
+                bending_hinge_block(cx.rel(q0.x), zero, cx.rel(q0.y & 0xffff), cx.rel(q0.y >> 16), __int_as_float(q0.z),
+                                    __int_as_float(q0.w), acc);
+                bending_hinge_block(cx.rel(q1.x), zero, cx.rel(q1.y & 0xffff), cx.rel(q1.y >> 16), __int_as_float(q1.z),
+                                    i1 < n ? __int_as_float(q1.w) : 0.f, acc);
             }
         }
         off += n;
