@@ -161,9 +161,9 @@ def _measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def _traffic_per_iteration():
-    """DRAM bytes per colour sweep from the committed ncu summary, when present."""
-    p = os.path.join(ROOT, "profiles", "vbd_color_kernel_spring_cloth_513.json")
+def _traffic_per_iteration(kernel_name):
+    """DRAM bytes per colour sweep of the given kernel from its committed ncu summary, when present."""
+    p = os.path.join(ROOT, "profiles", f"{kernel_name}_spring_cloth_513.json")
     try:
         with open(p) as f:
             return float(json.load(f)["dram_bytes_per_sweep"])
@@ -196,6 +196,72 @@ def cpu_baseline(target_s: float = 12.0) -> dict:
     return {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{c} colour phases ({done} vertex-solves, {c / ncol:.2f} sweeps) of the 513x513 cloth, "
                       f"full-element FP64 AD per incidence, {dt:.1f} s"}
+
+
+def time_to_residual(local, tol=1e-5, prefix=2, steps=3, max_iterations=40000, warm=None) -> dict:
+    """Wall time of VBD steps run to ||M/h^2 (x - y) + grad E(x)|| <= tol ||grad E(y)|| (FP64-reduced
+    residual, checked every 200 iterations) on the 513x513 cloth. A fresh solver starts from rest;
+    the first `prefix` steps build the displacement history and are not timed; the next `steps`
+    steps are timed with CUDA events on the solver's stream. `warm` (an MLP handle) switches the
+    learned initial guess on for every step of the run; None keeps the inertial guess."""
+    from spg_gb300 import native as N
+    from spg_gb300 import scenes as S
+    obj = S.spring_cloth(ROWS).objects[0]
+    solver = N.VbdSolver([obj], dt=DT, iterations=ITERATIONS, gravity=GRAVITY, device=local,
+                         tolerance=tol, max_iterations=max_iterations, check_interval=200)
+    if warm is not None:
+        solver.set_warm_start(warm)
+    rows = []
+    for k in range(prefix + steps):
+        st = solver.step()
+        if k >= prefix:
+            rows.append({"iterations": int(st.iterations), "converged": bool(st.converged),
+                         "device_ms": float(st.device_ms),
+                         "relative_residual": st.residual_final / st.residual_initial,
+                         "warm_accepted": int(getattr(st, "warm_accepted", 0))})
+    solver.close()
+    return {"ms_total": sum(r["device_ms"] for r in rows), "steps": rows}
+
+
+def _timed_steps(solver, steps):
+    for _ in range(3):
+        solver.step()
+    return [solver.step().device_ms for _ in range(steps)]
+
+
+def other_configs(local) -> dict:
+    """The other benchmark configurations, each timed with CUDA events on its solver's stream
+    (vertex-solves/s = vertices x iterations / device time; XPBD in steps/s)."""
+    from spg_gb300 import native as N
+    from spg_gb300 import scenes as S
+    out = {}
+    cloth = S.cloth(33).objects[0]
+    s = N.VbdSolver([cloth], dt=1 / 60, iterations=100, gravity=GRAVITY, device=local)
+    ms = statistics.mean(_timed_steps(s, 10))
+    out["cloth_33x33_stvk_100it"] = {"vertex_solves_per_s": cloth.nv * 100 / (ms * 1e-3), "ms_per_step": ms,
+                                     "launch": list(s.launch())}
+    s.close()
+    beam = S.tet_beam().objects[0]
+    s = N.VbdSolver([beam], dt=1 / 60, iterations=50, gravity=GRAVITY, device=local)
+    ms = statistics.mean(_timed_steps(s, 10))
+    out["snh_beam_41x11x11_50it"] = {"vertex_solves_per_s": beam.nv * 50 / (ms * 1e-3), "ms_per_step": ms,
+                                     "launch": list(s.launch())}
+    s.close()
+    batch = S.patch_batch(512, 16, 128, seed=2024).objects
+    nv = sum(o.nv for o in batch)
+    s = N.VbdSolver(batch, dt=1 / 60, iterations=30, gravity=GRAVITY, device=local)
+    ms = statistics.mean(_timed_steps(s, 5))
+    out["batch_512_patches_30it"] = {"vertex_solves_per_s": nv * 30 / (ms * 1e-3), "ms_per_step": ms,
+                                     "vertices": nv, "colors": int(s.n_colors(-1)), "launch": list(s.launch()),
+                                     "graph": True}
+    s.close()
+    big = S.spring_cloth(ROWS).objects[0]
+    x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local)
+    ms = statistics.mean(_timed_steps(x, 5))
+    out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
+                                               "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3)}
+    x.close()
+    return out
 
 
 def run_reference(args, dist, rank, local, ws):
@@ -294,7 +360,8 @@ def run_gb300(args, dist, rank, local, ws):
     alg_bytes = algorithmic_bytes_per_iteration(obj)
     peak, peak_kind = _measured_peaks()
     achieved = alg_bytes / sweep_s / 1e9
-    traffic = _traffic_per_iteration()
+    kernel_name = "vbd_color_kernel" if kernel == 1 else "vbd_tile_kernel"
+    traffic = _traffic_per_iteration(kernel_name)
 
     if rank != 0:
         return 0
@@ -304,7 +371,8 @@ def run_gb300(args, dist, rank, local, ws):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB write)",
                    "kernel": {1: "lanes-per-vertex", 2: "shared-memory tiles"}[kernel],
-                   "lanes_per_vertex" if kernel == 1 else "tile_vertices": lanes, "block_size": block,
+                   "lanes_per_vertex": lanes, "block_size": block,
+                   "tile_vertices": (solver.params.tile_vertices or 64) if kernel == 2 else None,
                    "colors": int(solver.n_colors(-1)),
                    "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
         "gpu_launches": launches_per_step * args.steps,
@@ -312,12 +380,18 @@ def run_gb300(args, dist, rank, local, ws):
                 "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "vbd_color_kernel" if kernel == 1 else "vbd_tile_kernel",
+                     "kernel": kernel_name,
                      "algorithmic_bytes_per_sweep": alg_bytes,
                      "bytes_per_vertex_solve": alg_bytes / nv, "sweep_ms": 1e3 * sweep_s,
                      "color_launch_ms": [round(float(c), 5) for c in color_ms]},
         "clocks": clocks,
     }
+    if not args.skip_extras:
+        ttr = time_to_residual(local)
+        line["time_to_residual"] = {"tolerance": 1e-5, "normaliser": "||grad E(y)|| at the inertial guess y",
+                                    "protocol": "fresh solver from rest; 2 untimed steps, then 3 timed steps",
+                                    "check_interval": 200, "plain": ttr}
+        line["configs"] = other_configs(local)
     if ws == 1 and not args.skip_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)
@@ -331,6 +405,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-extras", action="store_true", help="skip time-to-residual and the other configs")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0 = autotune)")
     ap.add_argument("--kernel", type=int, default=0, help="1 = lanes per vertex, 2 = tiles (0 = autotune)")
