@@ -142,6 +142,9 @@ typedef struct spgx_step_stats {
     double residual_initial;   /* ||r(y)|| of the last substep (tolerance mode, else 0) */
     double residual_final;     /* ||r(x)|| at the end of the last substep (tolerance mode) */
     double device_ms;          /* CUDA-event time of the step on the handle's stream */
+    int32_t warm_accepted;     /* substeps whose learned initial guess was kept */
+    int32_t reserved0;
+    double residual_warm;      /* ||r(x_w)|| of the learned guess of the last substep (tolerance mode) */
 } spgx_step_stats;
 
 /*
@@ -189,6 +192,61 @@ spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *kernel, int32_t *lanes_per
  * (spgx_vbd_num_colors(h, -1, ...) entries). Advances the positions like the iterations of
  * a step (no inertial or velocity phase). */
 spgx_status spgx_vbd_profile_sweeps(spgx_vbd *h, int32_t iterations, double *color_ms);
+
+/* ------------------------------------------------------------------------------------ */
+/* Learned warm start. No counterpart in the reference, whose only initial guess is the
+ * inertial one (vbd.h:22, InitialGuessType::InertialWithAcceleration; vbd.cpp:78-83).
+ *
+ * A per-vertex MLP (24 -> 128 -> 128 -> 128 -> 3, GELU; BF16 weights on the tensor cores with
+ * FP32 accumulation) maps local features of the displacement history to the offset of the
+ * step's solution from the inertial guess y, in units of l = h^2 * 9.81 m/s^2. Features per
+ * vertex (24 floats, displacements over l): y - x_n, x_n - x_{n-1}, x_{n-1} - x_{n-2}, the
+ * one-ring Laplacians (neighbour mean minus own) of the last two, g / 9.81, the anchored
+ * flag, the anchored fraction of the one-ring, the one-ring size / 8, |x_n - x_{n-1}|,
+ * |Laplacian of x_n - x_{n-1}| and 1.
+ *
+ * With the warm start enabled every substep evaluates the candidate x_w = y + l * MLP and
+ * keeps it only when ||r(x_w)|| < ||r(y)|| (both FP64-reduced on the device); otherwise the
+ * substep starts from y. The tolerance test stays relative to ||r(y)||, so the guess cannot
+ * loosen it. */
+
+typedef struct spgx_mlp spgx_mlp;
+
+/* Parameter count and layout of the flat FP32 weight vector: W1[24][128] b1[128]
+ * W2[128][128] b2[128] W3[128][128] b3[128] W4[128][3] b4[3] (row-major, input-major). */
+int32_t spgx_mlp_num_params(void);
+/* New network with Xavier-uniform weights drawn from `seed` and zero biases. */
+spgx_status spgx_mlp_create(uint64_t seed, int32_t device, spgx_mlp **out);
+spgx_status spgx_mlp_destroy(spgx_mlp *h);
+spgx_status spgx_mlp_get_weights(spgx_mlp *h, float *w);
+/* Replaces the weights (FP32 master copy; inference uses their BF16 rounding) and clears the
+ * optimizer state. */
+spgx_status spgx_mlp_set_weights(spgx_mlp *h, const float *w);
+/* y[n][3] = MLP(x[n][24]) on the tensor cores (host arrays). */
+spgx_status spgx_mlp_forward(spgx_mlp *h, int32_t n, const float *x, float *y);
+/* Mean squared error over the n x 3 outputs against y, and its gradient with respect to the
+ * flat weights (FP32 forward/backward with the BF16-rounded weights; the rounding is passed
+ * straight through). grad has spgx_mlp_num_params() entries. */
+spgx_status spgx_mlp_loss_grad(spgx_mlp *h, int32_t n, const float *x, const float *y, float *loss, float *grad);
+/* `steps` Adam steps (beta 0.9 / 0.999, eps 1e-8, learning rate lr) on minibatches of `batch`
+ * rows drawn uniformly with replacement (seeded) from the n rows; all on the device.
+ * final_loss (may be NULL) is the last minibatch's loss. */
+spgx_status spgx_mlp_train(spgx_mlp *h, int32_t n, const float *x, const float *y, int32_t steps, int32_t batch,
+                           float lr, uint64_t seed, float *final_loss);
+
+/* Attaches the network to a solver (mlp may be NULL with enable 0). The first call also
+ * starts keeping the displacement history (from then on, and after every set_state/reset,
+ * seeded with a constant-velocity past). The network must outlive its use by the solver and
+ * live on the solver's device; do not train it while the solver steps. */
+spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t enable);
+/* One step (one substep only; history started by spgx_vbd_set_warm_start) that also returns,
+ * for every vertex of the scene in the solver's internal order, the features at the start of
+ * the step (features[n_vertices][24]) and the training target (x - y) / l at its end
+ * (targets[n_vertices][3]). */
+spgx_status spgx_vbd_step_record(spgx_vbd *h, float *features, float *targets, spgx_step_stats *stats);
+/* The solver's internal vertex order (colour-major): ext_of_internal[i] is the index, in the
+ * scene's concatenated object-by-object vertex order, of internal vertex i. */
+spgx_status spgx_vbd_get_vertex_order(spgx_vbd *h, int32_t *ext_of_internal);
 
 /* ------------------------------------------------------------------------------------ */
 /* Element-level evaluation on the GPU with the solver's device code (FP32), for the

@@ -51,6 +51,19 @@ __global__ void end_substep_kernel(const float4 *pos, const float4 *dold, float4
     vel[i] = make_float4((d.x - o.x) * invh, (d.y - o.y) * invh, (d.z - o.z) * invh, 0.f);
 }
 
+// The same update, first saving the previous velocity v_n (vel - h g) as history.
+__global__ void end_substep_hist_kernel(const float4 *pos, const float4 *dold, float4 *vel, float4 *vhist, int nv,
+                                        float invh, float ghx, float ghy, float ghz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const float4 u = vel[i];
+    vhist[i] = make_float4(u.x - ghx, u.y - ghy, u.z - ghz, 0.f);
+    const float4 d = pos[2 * i + 1];
+    const float4 o = dold[i];
+    vel[i] = make_float4((d.x - o.x) * invh, (d.y - o.y) * invh, (d.z - o.z) * invh, 0.f);
+}
+
 void launch_begin_substep(const ParticleState &P, double h, const double *g, cudaStream_t st)
 {
     if (P.nv == 0) return;
@@ -58,9 +71,15 @@ void launch_begin_substep(const ParticleState &P, double h, const double *g, cud
                                                              float(g[0]), float(g[1]), float(g[2]));
 }
 
-void launch_end_substep(const ParticleState &P, double h, cudaStream_t st)
+void launch_end_substep(const ParticleState &P, double h, cudaStream_t st, float4 *vhist, const double *g)
 {
     if (P.nv == 0) return;
+    if (vhist) {
+        end_substep_hist_kernel<<<(P.nv + 255) / 256, 256, 0, st>>>(P.pos(), P.dold(), P.vel(), vhist, P.nv,
+                                                                    float(1.0 / h), float(h * g[0]), float(h * g[1]),
+                                                                    float(h * g[2]));
+        return;
+    }
     end_substep_kernel<<<(P.nv + 255) / 256, 256, 0, st>>>(P.pos(), P.dold(), P.vel(), P.nv, float(1.0 / h));
 }
 

@@ -37,6 +37,9 @@ struct ParticleState {
 
 // Substep kernels shared by both solvers (see state.cu).
 void launch_begin_substep(const ParticleState &P, double h, const double *g, cudaStream_t st);
-void launch_end_substep(const ParticleState &P, double h, cudaStream_t st);
+// With vhist given, also stores v_n = (velocity after the inertial predict) - h g into vhist
+// before the velocity update (the displacement history of the learned warm start).
+void launch_end_substep(const ParticleState &P, double h, cudaStream_t st, float4 *vhist = nullptr,
+                        const double *g = nullptr);
 
 }  // namespace spgx

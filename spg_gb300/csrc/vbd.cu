@@ -15,6 +15,7 @@
 #include "device_common.cuh"
 #include "layout.h"
 #include "state.h"
+#include "mlp.h"
 #include "vbd_solver.h"
 
 namespace spgx {
@@ -291,13 +292,17 @@ static void launch_iterations(const VbdSolver &s, int n, cudaStream_t st)
 
 static void launch_begin(const VbdSolver &s, cudaStream_t st) { launch_begin_substep(s.X, s.h_sub, s.P.gravity, st); }
 
-static void launch_end(const VbdSolver &s, cudaStream_t st) { launch_end_substep(s.X, s.h_sub, st); }
+static void launch_end(const VbdSolver &s, cudaStream_t st)
+{
+    launch_end_substep(s.X, s.h_sub, st, s.W.history ? s.W.vhist.as<float4>() : nullptr, s.P.gravity);
+}
 
-static void launch_residual(const VbdSolver &s, cudaStream_t st)
+// Adds ||r(x)||^2 of the current positions to *out (default: the handle's residual slot).
+static void launch_residual(const VbdSolver &s, cudaStream_t st, double *out = nullptr)
 {
     if (s.L.nv == 0) return;
     const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
-    double *out = s.d_resid.as<double>();
+    if (!out) out = s.d_resid.as<double>();
     if (s.kernel == 2) {
         const int nt = s.TL.color_tiles.back();
         const int threads = s.TL.tile_vertices * s.lanes;
@@ -563,6 +568,7 @@ spgx_status VbdSolver::build_graph()
     SPGX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < P.substeps; ++s) {
         launch_begin(*this, stream);
+        if (W.enabled) launch_warm(stream);
         launch_iterations(*this, P.iterations, stream);
         launch_end(*this, stream);
     }
@@ -621,20 +627,97 @@ spgx_status VbdSolver::residual_norm(double *out)
     return SPGX_OK;
 }
 
-spgx_status VbdSolver::step(spgx_step_stats *stats)
+// Learned initial guess of one substep, after the inertial predict (all on the stream, no host
+// round trip): wres[0] = ||r(y)||^2, the MLP's candidate x_w = y + l * MLP(features),
+// wres[1] = ||r(x_w)||^2, and x_w is kept only when its residual is lower.
+void VbdSolver::launch_warm(cudaStream_t st)
 {
+    double *wres = W.wres.as<double>();
+    cudaMemsetAsync(wres, 0, 2 * sizeof(double), st);
+    launch_residual(*this, st, wres);
+    launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, st);
+    W.mlp->infer(W.feats.as<float>(), L.nv, W.out.as<float>(), st);
+    launch_warm_apply(W, X.pos(), X.tgt(), L.nv, h_sub, st);
+    launch_residual(*this, st, wres + 1);
+    launch_warm_select(W, X.pos(), X.tgt(), L.nv, d_counters.as<int>() + 3, st);
+}
+
+// Uploads positions/velocities set from the host; a replaced state restarts the displacement
+// history at constant velocity.
+spgx_status VbdSolver::upload_state()
+{
+    const bool replaced = X.device_dirty;
     SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+    if (replaced && W.history)
+        SPGX_CUDA(cudaMemcpyAsync(W.vhist.as<void>(), X.vel(), size_t(L.nv) * sizeof(float4),
+                                  cudaMemcpyDeviceToDevice, stream));
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::enable_history()
+{
+    if (W.history) return SPGX_OK;
+    std::vector<int32_t> off, nbr;
+    std::vector<F4> stat;
+    build_vertex_neighbours(L, off, nbr, stat);
+    if (nbr.empty()) nbr.push_back(0);
+    SPGX_TRY_STATUS(W.nbr_off.upload(off));
+    SPGX_TRY_STATUS(W.nbr.upload(nbr));
+    SPGX_TRY_STATUS(W.stat.upload(stat));
+    const size_t n = size_t(std::max(1, L.nv));
+    SPGX_TRY_STATUS(W.vhist.alloc(n * sizeof(float4)));
+    SPGX_TRY_STATUS(W.feats.alloc(n * kWarmFeatures * sizeof(float)));
+    SPGX_TRY_STATUS(W.out.alloc(n * 3 * sizeof(float)));
+    SPGX_TRY_STATUS(W.wres.alloc(2 * sizeof(double)));
+    // No earlier motion is known: take the previous step's displacement equal to the current
+    // velocity's (constant-velocity history).
+    SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+    SPGX_CUDA(cudaMemcpyAsync(W.vhist.as<void>(), X.vel(), size_t(L.nv) * sizeof(float4), cudaMemcpyDeviceToDevice,
+                              stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    W.history = true;
+    graph_valid = false;
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::set_warm_start(const Mlp *mlp, bool enable)
+{
+    if (enable && !mlp) {
+        set_error("enabling the warm start needs an MLP handle");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (mlp && mlp->device != device) {
+        set_error("the MLP handle lives on another device than the solver");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_TRY_STATUS(enable_history());
+    W.mlp = mlp;
+    W.enabled = enable;
+    graph_valid = false;
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targets)
+{
+    const bool record = features || targets;
+    if (record && (P.substeps != 1 || !W.history)) {
+        set_error("recording needs one substep and the displacement history (spgx_vbd_set_warm_start)");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_TRY_STATUS(upload_state());
     X.mark_device_advanced();
     spgx_step_stats st{};
     SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, 4 * sizeof(int), stream));
     SPGX_CUDA(cudaEventRecord(ev0, stream));
-    if (P.tolerance <= 0) {
+    double *hw = reinterpret_cast<double *>(h_counters.as<int>() + 4);  // 2 doubles of pinned scratch
+    if (P.tolerance <= 0 && !record) {
         if (P.use_graph) {
             if (!graph_valid) SPGX_TRY_STATUS(build_graph());
             SPGX_CUDA(cudaGraphLaunch(graph_exec, stream));
         } else {
             for (int s = 0; s < P.substeps; ++s) {
                 launch_begin(*this, stream);
+                if (W.enabled) launch_warm(stream);
                 launch_iterations(*this, P.iterations, stream);
                 launch_end(*this, stream);
             }
@@ -646,32 +729,56 @@ spgx_status VbdSolver::step(spgx_step_stats *stats)
         for (int s = 0; s < P.substeps; ++s) {
             launch_begin(*this, stream);
             double r0 = 0, r = 0;
-            SPGX_TRY_STATUS(residual_norm(&r0));
-            r = r0;
-            int it = 0;
-            while (it < P.max_iterations && r > P.tolerance * r0) {
-                const int chunk = std::min(P.check_interval, P.max_iterations - it);
-                launch_iterations(*this, chunk, stream);
-                it += chunk;
-                SPGX_TRY_STATUS(residual_norm(&r));
+            if (W.enabled) {
+                launch_warm(stream);
+                SPGX_CUDA(cudaMemcpyAsync(hw, W.wres.as<double>(), 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                          stream));
+                SPGX_CUDA(cudaStreamSynchronize(stream));
+                r0 = std::sqrt(hw[0]);
+                st.residual_warm = std::sqrt(hw[1]);
+                r = hw[1] < hw[0] ? st.residual_warm : r0;
+            } else {
+                if (record) launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, stream);
+                if (P.tolerance > 0) SPGX_TRY_STATUS(residual_norm(&r0));
+                r = r0;
             }
-            if (r > P.tolerance * r0) st.converged = 0;
+            if (P.tolerance > 0) {
+                int it = 0;
+                while (it < P.max_iterations && r > P.tolerance * r0) {
+                    const int chunk = std::min(P.check_interval, P.max_iterations - it);
+                    launch_iterations(*this, chunk, stream);
+                    it += chunk;
+                    SPGX_TRY_STATUS(residual_norm(&r));
+                }
+                if (r > P.tolerance * r0) st.converged = 0;
+                st.iterations += it;
+                st.residual_initial = r0;
+                st.residual_final = r;
+            } else {
+                launch_iterations(*this, P.iterations, stream);
+                st.iterations += P.iterations;
+            }
+            if (record) launch_warm_targets(X.pos(), X.tgt(), L.nv, h_sub, W.out.as<float>(), stream);
             launch_end(*this, stream);
-            st.iterations += it;
-            st.residual_initial = r0;
-            st.residual_final = r;
         }
     }
     SPGX_CUDA(cudaEventRecord(ev1, stream));
     SPGX_CUDA(cudaGetLastError());
     int *hc = h_counters.as<int>();
     SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    if (features)
+        SPGX_CUDA(cudaMemcpyAsync(features, W.feats.as<float>(), size_t(L.nv) * kWarmFeatures * sizeof(float),
+                                  cudaMemcpyDeviceToHost, stream));
+    if (targets)
+        SPGX_CUDA(cudaMemcpyAsync(targets, W.out.as<float>(), size_t(L.nv) * 3 * sizeof(float),
+                                  cudaMemcpyDeviceToHost, stream));
     SPGX_CUDA(cudaStreamSynchronize(stream));
     float ms = 0.f;
     SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     st.device_ms = ms;
     st.fallback_solves = hc[0];
     st.skipped_solves = hc[1];
+    st.warm_accepted = hc[3];
     if (stats) *stats = st;
     if (hc[2] & 1u) {
         set_error("a vertex update produced a non-finite position; the update was not stored");
@@ -792,8 +899,46 @@ spgx_status spgx_vbd_residual(spgx_vbd *h, double *norm)
         spgx::set_error("norm is NULL");
         return SPGX_ERR_INVALID_ARG;
     }
-    SPGX_TRY_STATUS(h->s->X.upload_if_dirty(h->s->stream));
+    SPGX_TRY_STATUS(h->s->upload_state());
     return h->s->residual_norm(norm);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t enable)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    if (enable != 0 && enable != 1) {
+        spgx::set_error("enable must be 0 or 1");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    return h->s->set_warm_start(mlp ? mlp->m.get() : nullptr, enable == 1);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_get_vertex_order(spgx_vbd *h, int32_t *ext_of_internal)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    if (!ext_of_internal) {
+        spgx::set_error("ext_of_internal is NULL");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    const auto &L = h->s->L;
+    std::copy(L.int2ext.begin(), L.int2ext.end(), ext_of_internal);
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_step_record(spgx_vbd *h, float *features, float *targets, spgx_step_stats *stats)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_HANDLE(h);
+    if (!features || !targets) {
+        spgx::set_error("features and targets must not be NULL");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    return h->s->step(stats, features, targets);
     SPGX_GUARD_END
 }
 

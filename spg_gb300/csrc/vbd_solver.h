@@ -8,6 +8,7 @@
 #include "layout.h"
 #include "state.h"
 #include "vbd_tile.cuh"
+#include "warm.h"
 
 namespace spgx {
 
@@ -41,6 +42,7 @@ struct VbdSolver {
     DevBuf tb_hdr, tb_halo, tb_records, tb_vrec;
     TileView TV{};
     size_t tile_smem{0};
+    WarmStart W;
 
     VbdSolver() = default;
     VbdSolver(const VbdSolver &) = delete;
@@ -55,7 +57,13 @@ struct VbdSolver {
     spgx_status build_graph();
     spgx_status residual_norm(double *out);
     spgx_status profile_sweeps(int iterations, double *color_ms);
-    spgx_status step(spgx_step_stats *stats);
+    // One step. With features/targets given (one substep only), also returns every vertex's
+    // warm-start features at the start of the step and its target (x* - y) / l at the end.
+    spgx_status step(spgx_step_stats *stats, float *features = nullptr, float *targets = nullptr);
+    spgx_status enable_history();
+    spgx_status upload_state();
+    spgx_status set_warm_start(const Mlp *mlp, bool enable);
+    void launch_warm(cudaStream_t st);
 };
 
 }  // namespace spgx

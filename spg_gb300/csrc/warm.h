@@ -1,0 +1,54 @@
+// Learned warm start of a VBD step: per-vertex features of the displacement history, the
+// MLP's predicted correction to the inertial guess, and the residual-based acceptance.
+//
+// Units: displacements are scaled by 1 / l with l = h^2 * kWarmG0 (the distance standard
+// gravity moves a body in one substep), so the features of a given motion do not depend on h.
+//
+// Features of vertex i (24 floats), with d_in = y - x_n (inertial displacement),
+// d1 = x_n - x_{n-1}, d2 = x_{n-1} - x_{n-2}, lap(u)_i = mean over the one-ring j of u_j - u_i:
+//   0-2  d_in / l          3-5  d1 / l           6-8   d2 / l
+//   9-11 lap(d1) / l       12-14 lap(d2) / l     15-17 g / kWarmG0
+//   18   anchored flag     19   anchored fraction of the one-ring
+//   20   one-ring size / 8 21   |d1| / l         22    |lap(d1)| / l     23  1
+// The one-ring is every vertex sharing a mesh edge, a triangle or a tet with i (the two
+// opposite vertices of a bending stencil are not neighbours of each other).
+// Target and output: (x* - y) / l, the converged position's offset from the inertial guess.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "devbuf.h"
+#include "layout.h"
+
+namespace spgx {
+
+constexpr int kWarmFeatures = 24;
+constexpr double kWarmG0 = 9.81;
+
+struct Mlp;
+
+// One-ring CSR in internal vertex order plus per-vertex static features
+// {anchored, anchored fraction of the one-ring, one-ring size / 8, 0}.
+void build_vertex_neighbours(const SceneLayout &L, std::vector<int32_t> &off, std::vector<int32_t> &nbr,
+                             std::vector<F4> &stat);
+
+struct WarmStart {
+    bool history{false};  // history buffers exist and are maintained every substep
+    bool enabled{false};  // the learned guess is tried at the start of every substep
+    const Mlp *mlp{nullptr};
+    DevBuf nbr_off, nbr, stat, vhist, feats, out, wres;
+};
+
+// feats = features of every vertex at the start of the substep (after the inertial predict).
+void launch_warm_features(const WarmStart &W, const float4 *vel, int nv, double h, const double *g, cudaStream_t st);
+// delta = tgt + l * out for every vertex (the candidate guess).
+void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, int nv, double h, cudaStream_t st);
+// Keeps the candidate when wres[1] < wres[0] (squared residual norms at the candidate and at
+// y), else restores delta = tgt; adds 1 to *accepted when kept.
+void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, int nv, int *accepted, cudaStream_t st);
+// targets = (x - y) / l for every vertex (training data of the converged step).
+void launch_warm_targets(const float4 *pos, const float4 *tgt, int nv, double h, float *targets, cudaStream_t st);
+
+}  // namespace spgx

@@ -58,7 +58,8 @@ class XpbdParams(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("fallback_solves", C.c_int32), ("skipped_solves", C.c_int32),
                 ("converged", C.c_int32), ("residual_initial", C.c_double), ("residual_final", C.c_double),
-                ("device_ms", C.c_double)]
+                ("device_ms", C.c_double), ("warm_accepted", C.c_int32), ("reserved0", C.c_int32),
+                ("residual_warm", C.c_double)]
 
 
 _lib = None
@@ -107,6 +108,18 @@ def lib():
         L.spgx_color_vertices.argtypes = [C.POINTER(ObjectDesc), ip]
         L.spgx_color_stencils.argtypes = [C.POINTER(EnergyDesc), ip]
         L.spgx_incidences.argtypes = [C.POINTER(ObjectDesc), ip, ip, C.POINTER(C.c_int64)]
+        fp = C.POINTER(C.c_float)
+        L.spgx_mlp_num_params.restype = i32
+        L.spgx_mlp_create.argtypes = [C.c_uint64, i32, C.POINTER(vp)]
+        L.spgx_mlp_destroy.argtypes = [vp]
+        L.spgx_mlp_get_weights.argtypes = [vp, fp]
+        L.spgx_mlp_set_weights.argtypes = [vp, fp]
+        L.spgx_mlp_forward.argtypes = [vp, i32, fp, fp]
+        L.spgx_mlp_loss_grad.argtypes = [vp, i32, fp, fp, fp, fp]
+        L.spgx_mlp_train.argtypes = [vp, i32, fp, fp, i32, i32, C.c_float, C.c_uint64, fp]
+        L.spgx_vbd_set_warm_start.argtypes = [vp, vp, i32]
+        L.spgx_vbd_step_record.argtypes = [vp, fp, fp, C.POINTER(StepStats)]
+        L.spgx_vbd_get_vertex_order.argtypes = [vp, ip]
         _lib = L
     return _lib
 
@@ -241,11 +254,91 @@ class VbdSolver:
         check(lib().spgx_vbd_profile_sweeps(self.h, iterations, _p(out, C.c_double)))
         return out
 
+    def set_warm_start(self, mlp=None, enable=True):
+        """Attaches `mlp` (an Mlp) as the learned initial guess; also starts the displacement
+        history. enable=False keeps the history but uses the inertial guess."""
+        self._mlp = mlp
+        check(lib().spgx_vbd_set_warm_start(self.h, None if mlp is None else mlp.h, 1 if enable else 0))
+
+    def step_record(self):
+        """One step returning (stats, features [n x 24], targets [n x 3]) in internal vertex order."""
+        n = sum(self.objects_nv)
+        f = np.zeros((n, WARM_FEATURES), np.float32)
+        t = np.zeros((n, 3), np.float32)
+        st = StepStats()
+        check(lib().spgx_vbd_step_record(self.h, _p(f, C.c_float), _p(t, C.c_float), C.byref(st)))
+        return st, f, t
+
+    def vertex_order(self) -> np.ndarray:
+        """ext_of_internal: scene vertex index (objects concatenated) of each internal row."""
+        out = np.zeros(sum(self.objects_nv), np.int32)
+        check(lib().spgx_vbd_get_vertex_order(self.h, _p(out, C.c_int32)))
+        return out
+
     def launch(self):
         """(kernel, lanes_per_vertex or tile vertices, block size) chosen by the solver."""
         k, g, b = C.c_int32(), C.c_int32(), C.c_int32()
         check(lib().spgx_vbd_get_launch(self.h, C.byref(k), C.byref(g), C.byref(b)))
         return k.value, g.value, b.value
+
+
+WARM_FEATURES = 24
+
+
+class Mlp:
+    """The warm-start network (24 -> 128 -> 128 -> 128 -> 3, GELU) on one GPU."""
+
+    def __init__(self, seed=0, device=0, weights=None):
+        h = C.c_void_p()
+        check(lib().spgx_mlp_create(seed, device, C.byref(h)))
+        self.h = h
+        if weights is not None:
+            self.set_weights(weights)
+
+    @staticmethod
+    def num_params() -> int:
+        return lib().spgx_mlp_num_params()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().spgx_mlp_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def weights(self) -> np.ndarray:
+        w = np.zeros(self.num_params(), np.float32)
+        check(lib().spgx_mlp_get_weights(self.h, _p(w, C.c_float)))
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32).reshape(-1)
+        if w.size != self.num_params():
+            raise ValueError(f"expected {self.num_params()} weights, got {w.size}")
+        check(lib().spgx_mlp_set_weights(self.h, _p(w, C.c_float)))
+
+    def forward(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, WARM_FEATURES)
+        y = np.zeros((x.shape[0], 3), np.float32)
+        check(lib().spgx_mlp_forward(self.h, x.shape[0], _p(x, C.c_float), _p(y, C.c_float)))
+        return y
+
+    def loss_grad(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, WARM_FEATURES)
+        y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1, 3)
+        g = np.zeros(self.num_params(), np.float32)
+        loss = C.c_float()
+        check(lib().spgx_mlp_loss_grad(self.h, x.shape[0], _p(x, C.c_float), _p(y, C.c_float), C.byref(loss),
+                                       _p(g, C.c_float)))
+        return loss.value, g
+
+    def train(self, x, y, steps, batch=4096, lr=1e-3, seed=0) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, WARM_FEATURES)
+        y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1, 3)
+        loss = C.c_float()
+        check(lib().spgx_mlp_train(self.h, x.shape[0], _p(x, C.c_float), _p(y, C.c_float), steps, batch, lr, seed,
+                                   C.byref(loss)))
+        return loss.value
 
 
 class XpbdSolver:
