@@ -36,7 +36,7 @@ typedef enum spgx_status {
     SPGX_ERR_UNSUPPORTED_ENERGY = 2, /* energy type outside the five below */
     SPGX_ERR_CUDA = 3,               /* CUDA runtime error (message in spgx_last_error_string) */
     SPGX_ERR_NONFINITE = 4,          /* a vertex update produced NaN/Inf; the update was not stored */
-    SPGX_ERR_TIMEOUT = 5,            /* a bounded device-side wait gave up */
+    SPGX_ERR_TIMEOUT = 5,            /* a bounded device-side wait gave up (dataflow kernel) */
     SPGX_ERR_NO_DEVICE = 6           /* no CUDA device, or not an sm_103 device */
 } spgx_status;
 
@@ -125,8 +125,11 @@ typedef struct spgx_vbd_params {
     int32_t block_size;        /* 0 = autotune; else a multiple of 32 up to 256 (lanes kernel) */
     int32_t use_graph;         /* 1 = replay the iteration loop as a CUDA graph */
     int32_t device;            /* CUDA device ordinal */
-    int32_t kernel;            /* 0 = autotune, 1 = lanes-per-vertex kernel, 2 = shared-memory tile kernel */
-    int32_t tile_vertices;     /* vertices per tile of the tile kernel (1..128; 0 = 64) */
+    int32_t kernel;            /* 0 = autotune, 1 = lanes-per-vertex kernel, 2 = shared-memory tile kernel
+                                * (one launch per colour), 3 = dataflow tile kernel (one persistent
+                                * cooperative launch runs all sweeps; a tile starts as soon as its
+                                * neighbour tiles finished the sweeps it reads; no CUDA graph needed) */
+    int32_t tile_vertices;     /* vertices per tile of the tile kernels (1..128; 0 = 64) */
 } spgx_vbd_params;
 
 /* Defaults: dt 0.01, 1 substep, 1 iteration, gravity (0,-9.8,0) (baseSolver.h:36-38),
@@ -142,9 +145,11 @@ typedef struct spgx_step_stats {
     double residual_initial;   /* ||r(y)|| of the last substep (tolerance mode, else 0) */
     double residual_final;     /* ||r(x)|| at the end of the last substep (tolerance mode) */
     double device_ms;          /* CUDA-event time of the step on the handle's stream */
-    int32_t warm_accepted;     /* substeps whose learned initial guess was kept */
-    int32_t reserved0;
-    double residual_warm;      /* ||r(x_w)|| of the learned guess of the last substep (tolerance mode) */
+    int32_t warm_accepted;         /* substeps started from the learned guess */
+    int32_t extrapolated_accepted; /* substeps started from the extrapolated guess */
+    double residual_warm;          /* ||r|| of the last substep's learned guess (mode 1) or extrapolated
+                                    * guess (mode 2); tolerance mode */
+    double residual_extrapolated;  /* ||r|| of the last substep's extrapolated guess; tolerance mode */
 } spgx_step_stats;
 
 /*
@@ -184,13 +189,14 @@ spgx_status spgx_vbd_get_colors(spgx_vbd *h, int32_t object, int32_t *colors);
 /* Incidence lists in reference order: counts[v * n_energies + e] and, in the same order,
  * (stencilIdx, vertexIdxInStencil) pairs. Pass entries == NULL to query *total first. */
 spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts, int32_t *entries, int64_t *total);
-/* Launch configuration the solver uses (after autotuning): kernel 1 with lanes per vertex and
- * block size, or kernel 2 (tiles; lanes_per_vertex = vertices per tile, block = threads). */
+/* Launch configuration the solver uses (after autotuning): the kernel (1, 2 or 3), lanes per
+ * vertex and threads per CTA. */
 spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *kernel, int32_t *lanes_per_vertex, int32_t *block_size);
 /* Runs `iterations` colour sweeps with a CUDA event pair around every colour launch on the
  * handle's stream and writes the mean duration (ms) of each colour's launch to color_ms
  * (spgx_vbd_num_colors(h, -1, ...) entries). Advances the positions like the iterations of
- * a step (no inertial or velocity phase). */
+ * a step (no inertial or velocity phase). With kernel 3 there are no per-colour launches:
+ * color_ms[0] receives the mean time of a whole sweep and the other entries 0. */
 spgx_status spgx_vbd_profile_sweeps(spgx_vbd *h, int32_t iterations, double *color_ms);
 
 /* ------------------------------------------------------------------------------------ */
@@ -198,17 +204,20 @@ spgx_status spgx_vbd_profile_sweeps(spgx_vbd *h, int32_t iterations, double *col
  * inertial one (vbd.h:22, InitialGuessType::InertialWithAcceleration; vbd.cpp:78-83).
  *
  * A per-vertex MLP (24 -> 128 -> 128 -> 128 -> 3, GELU; BF16 weights on the tensor cores with
- * FP32 accumulation) maps local features of the displacement history to the offset of the
- * step's solution from the inertial guess y, in units of l = h^2 * 9.81 m/s^2. Features per
+ * FP32 accumulation) maps local features of the displacement history to a correction c of
+ * the extrapolated guess x_e = x_n + 2 (x_n - x_{n-1}) - (x_{n-1} - x_{n-2}) (the last
+ * step's acceleration carried over): x_w = x_e + l c, in units of l = h^2 * 9.81 m/s^2.
+ * Predicting only the remainder keeps the network's BF16 precision from limiting the guess.
+ * Features per
  * vertex (24 floats, displacements over l): y - x_n, x_n - x_{n-1}, x_{n-1} - x_{n-2}, the
  * one-ring Laplacians (neighbour mean minus own) of the last two, g / 9.81, the anchored
  * flag, the anchored fraction of the one-ring, the one-ring size / 8, |x_n - x_{n-1}|,
  * |Laplacian of x_n - x_{n-1}| and 1.
  *
- * With the warm start enabled every substep evaluates the candidate x_w = y + l * MLP and
- * keeps it only when ||r(x_w)|| < ||r(y)|| (both FP64-reduced on the device); otherwise the
- * substep starts from y. The tolerance test stays relative to ||r(y)||, so the guess cannot
- * loosen it. */
+ * With the learned warm start every substep evaluates y, x_e and x_w and starts from the one
+ * with the lowest ||r|| (FP64-reduced on the device), so the network can only help; a guess
+ * is kept only when it lowers the residual below ||r(y)||. The tolerance test stays relative
+ * to ||r(y)||, so a guess cannot loosen it. */
 
 typedef struct spgx_mlp spgx_mlp;
 
@@ -234,15 +243,20 @@ spgx_status spgx_mlp_loss_grad(spgx_mlp *h, int32_t n, const float *x, const flo
 spgx_status spgx_mlp_train(spgx_mlp *h, int32_t n, const float *x, const float *y, int32_t steps, int32_t batch,
                            float lr, uint64_t seed, float *final_loss);
 
-/* Attaches the network to a solver (mlp may be NULL with enable 0). The first call also
- * starts keeping the displacement history (from then on, and after every set_state/reset,
- * seeded with a constant-velocity past). The network must outlive its use by the solver and
- * live on the solver's device; do not train it while the solver steps. */
-spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t enable);
+/* Chooses the initial guess of every substep: mode 0 the inertial guess y (the reference's);
+ * mode 1 the learned guess (mlp required); mode 2 the previous step's acceleration carried
+ * over, x_w = x_n + 2 (x_n - x_{n-1}) - (x_{n-1} - x_{n-2}) (no network; a baseline for
+ * the learned guess). Modes 1 and 2 keep their candidate only when it lowers the residual.
+ * The first call also starts keeping the displacement history (from then on, and after
+ * every set_state/reset, seeded with a constant-velocity past). The network must outlive
+ * its use by the solver and live on the solver's device; do not train it while the solver
+ * steps. */
+spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t mode);
 /* One step (one substep only; history started by spgx_vbd_set_warm_start) that also returns,
  * for every vertex of the scene in the solver's internal order, the features at the start of
- * the step (features[n_vertices][24]) and the training target (x - y) / l at its end
- * (targets[n_vertices][3]). */
+ * the step (features[n_vertices][24]) and (x - y) / l at its end (targets[n_vertices][3]);
+ * the network's training target is that minus (features[3:6] - features[6:9] -
+ * features[15:18]), the extrapolated guess's offset from y. */
 spgx_status spgx_vbd_step_record(spgx_vbd *h, float *features, float *targets, spgx_step_stats *stats);
 /* The solver's internal vertex order (colour-major): ext_of_internal[i] is the index, in the
  * scene's concatenated object-by-object vertex order, of internal vertex i. */

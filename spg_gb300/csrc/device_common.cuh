@@ -39,6 +39,8 @@ struct DevTables {
     const float2 *anchor_cmp;
 };
 
+constexpr int kCounters = 8;
+
 struct DevState {
     float4 *pos;
     float4 *tgt;
@@ -46,8 +48,9 @@ struct DevState {
     float4 *vel;
     const int4 *hdr;
     const int *adj;
-    int *counters;          // [0] FP64 fallback solves, [1] det-guard skips
-    unsigned int *status;   // bit 0: non-finite update
+    int *counters;          // [0] FP64 fallback solves, [1] det-guard skips, [3] learned guesses kept,
+                            // [4] extrapolated guesses kept (kCounters ints; [2] is status)
+    unsigned int *status;   // bit 0: non-finite update, bit 1: a bounded wait gave up
 };
 
 typedef Vec3<float> V3f;
@@ -70,6 +73,24 @@ __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol
 // Lets the next kernel on the stream start launching once every CTA of this grid has called it
 // or exited (the next kernel still waits in wait_prior_grid for this grid's completion).
 __device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// GPU-scope acquire load / release store of a 32-bit counter (inter-CTA signalling).
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 
 // Walks the vertex's class-sorted incidence list with G lanes per vertex (lane-strided) and

@@ -142,6 +142,89 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
     if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], invdt2, fb2);
 }
 
+// Dataflow sweeps: a persistent kernel that runs `iterations` colour sweeps with no barrier
+// between colours. Every (iteration, tile) is one task, handed out in (iteration, colour,
+// tile) order by an atomic ticket. Tile T of colour c at iteration k may start when every
+// neighbour tile U (the tiles owning T's halo, and T itself) has finished iteration k if U's
+// colour is lower than c, and iteration k - 1 otherwise: exactly the reads Gauss-Seidel over
+// colours prescribes. Higher-colour neighbours cannot overwrite T's inputs early, because
+// they in turn wait for T. Each task waits only on tasks with smaller tickets, all held by
+// co-resident CTAs (cooperative launch), so the waits always end; each is still bounded, and
+// a wait that gives up sets the abort flag and status bit 1 so that every CTA leaves.
+constexpr int kFlowMaxPolls = 1 << 22;  // with 128 ns sleeps: about a second per wait
+
+template <int G>
+__global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V, const DevState S,
+                                                                const FlowView F, int n_tiles, int iterations,
+                                                                int epoch_base, int max_local, float invdt2,
+                                                                float fb2)
+{
+    extern __shared__ float4 dyn[];
+    float4 *sb = dyn;
+    float4 *sd = dyn + max_local;
+    int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
+    __shared__ int s_task, s_fail;
+    const int total = iterations * n_tiles;
+    const int lv = threadIdx.x / G;
+    const int lane = threadIdx.x & (G - 1);
+    for (;;) {
+        if (threadIdx.x == 0) s_task = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
+        __syncthreads();
+        const int task = s_task;
+        if (task >= total) break;
+        const int k = task / n_tiles;
+        const int tile = task - k * n_tiles;
+        if (threadIdx.x < 32) {
+            const int c = __ldg(F.tile_color + tile);
+            const int b = __ldg(F.nbr_off + tile), e = __ldg(F.nbr_off + tile + 1);
+            bool ok = true;
+            for (int j = b + threadIdx.x; j < e && ok; j += 32) {
+                const int u = __ldg(F.nbr + j);
+                const int need = epoch_base + k + (__ldg(F.tile_color + u) < c ? 1 : 0);
+                int polls = 0;
+                while (ld_acquire_gpu(F.epoch + u) < need) {
+                    if (++polls > kFlowMaxPolls || ld_relaxed_gpu(F.ticket + 1)) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+            }
+            ok = __all_sync(0xffffffffu, ok);
+            if (threadIdx.x == 0) s_fail = !ok;
+        }
+        __syncthreads();
+        if (s_fail) {
+            if (threadIdx.x == 0) {
+                atomicExch(F.ticket + 1, 1);
+                atomicOr(S.status, 2u);
+            }
+            break;
+        }
+        const int4 h0 = tile_stage(V, S.pos, tile, sb, sd, srec);
+        const bool active = lv < h0.y;
+        int4 hv = make_int4(0, 0, 0, 0);
+        int roff = 0;
+        TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
+        if (active) {
+            hv = __ldg(S.hdr + h0.x + lv);
+            roff = __ldg(V.vrec + h0.x + lv);
+            cx.bs = v3(sb[lv]);
+            cx.ds = v3(sd[lv]);
+        }
+        Block<float> acc;
+        block_zero(acc);
+        tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+        group_reduce<G>(acc);
+        if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], invdt2, fb2);
+        __syncthreads();  // every position of the tile is written (and the staging is consumed)
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release_gpu(F.epoch + tile, epoch_base + k + 1);
+        }
+    }
+}
+
 // Block-wide FP64 sum into *out (one atomic per block).
 __device__ __forceinline__ void block_sum_atomic(double v, double *out)
 {
@@ -284,8 +367,52 @@ static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
     }
 }
 
+// n sweeps of the dataflow kernel in one cooperative launch (one resident wave of CTAs).
+static void launch_flow(const VbdSolver &s, int n, cudaStream_t st)
+{
+    const int n_tiles = s.TL.color_tiles.back();
+    if (n <= 0 || n_tiles <= 0) return;
+    cudaMemsetAsync(s.FV.ticket, 0, 2 * sizeof(int), st);
+    const int li = s.lanes == 1 ? 0 : s.lanes == 2 ? 1 : s.lanes == 4 ? 2 : 3;
+    const long long tasks = static_cast<long long>(n) * n_tiles;
+    const int grid = static_cast<int>(std::min<long long>(tasks, static_cast<long long>(s.flow_blocks_per_sm[li]) *
+                                                                     s.num_sms));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(s.TL.tile_vertices * s.lanes);
+    cfg.dynamicSmemBytes = s.tile_smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
+    const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
+    const int base = s.flow_epoch;
+    cudaError_t e = cudaErrorInvalidConfiguration;  // warp 0 polls with full-warp votes: >= 32 threads
+    if (cfg.blockDim.x >= 32) {
+        switch (s.lanes) {
+        case 1: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<1>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
+        case 2: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<2>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
+        case 4: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<4>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
+        default: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<8>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
+        }
+    }
+    // The counters only advance when the sweeps were enqueued; a failed launch is reported by
+    // the caller's error check.
+    if (e == cudaSuccess)
+        s.flow_epoch += n;
+    else
+        s.flow_launch_error = e;
+}
+
 static void launch_iterations(const VbdSolver &s, int n, cudaStream_t st)
 {
+    if (s.kernel == 3) {
+        launch_flow(s, n, st);
+        return;
+    }
     for (int it = 0; it < n; ++it)
         for (int c = 0; c < s.L.n_colors; ++c) launch_color(s, c, st);
 }
@@ -303,7 +430,7 @@ static void launch_residual(const VbdSolver &s, cudaStream_t st, double *out = n
     if (s.L.nv == 0) return;
     const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
     if (!out) out = s.d_resid.as<double>();
-    if (s.kernel == 2) {
+    if (s.kernel >= 2) {
         const int nt = s.TL.color_tiles.back();
         const int threads = s.TL.tile_vertices * s.lanes;
         if (nt > 0) {
@@ -392,11 +519,11 @@ spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params 
     SPGX_TRY_STATUS(EB.upload(L.el, T));
     SPGX_TRY_STATUS(d_hdr.upload(L.hdr));
     SPGX_TRY_STATUS(d_adj.upload(L.adj));
-    SPGX_TRY_STATUS(d_counters.alloc(4 * sizeof(int)));
+    SPGX_TRY_STATUS(d_counters.alloc(kCounters * sizeof(int)));
     SPGX_TRY_STATUS(d_resid.alloc(2 * sizeof(double)));
     SPGX_TRY_STATUS(d_backup.alloc(size_t(L.nv) * 2 * sizeof(float4)));
-    SPGX_TRY_STATUS(h_counters.alloc(4 * sizeof(int) + 2 * sizeof(double)));
-    SPGX_CUDA(cudaMemset(d_counters.as<int>(), 0, 4 * sizeof(int)));
+    SPGX_TRY_STATUS(h_counters.alloc(kCounters * sizeof(int) + 4 * sizeof(double)));
+    SPGX_CUDA(cudaMemset(d_counters.as<int>(), 0, kCounters * sizeof(int)));
     S = DevState{};
     S.pos = X.pos();
     S.tgt = X.tgt();
@@ -407,6 +534,7 @@ spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params 
     S.counters = d_counters.as<int>();
     S.status = reinterpret_cast<unsigned int *>(d_counters.as<int>() + 2);
     SPGX_TRY_STATUS(setup_tiles());
+    SPGX_TRY_STATUS(setup_flow());
     SPGX_TRY_STATUS(configure_launch());
     return SPGX_OK;
 }
@@ -429,19 +557,101 @@ spgx_status VbdSolver::setup_tiles()
     TV.records = tb_records.as<int4>();
     TV.vrec = tb_vrec.as<int>();
     tile_smem = tile_smem_bytes(std::max(1, TL.max_local), std::max(1, TL.max_records));
-    if (tile_smem > 48 * 1024) {
-        auto raise = [this](const void *fn) -> cudaError_t {
-            return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tile_smem));
+    // The opt-in limit is declared once for every tile kernel, whatever this scene needs: the
+    // attribute is process-wide, so a per-scene value would break a larger scene's live
+    // handle, and the residual kernel's 256 B of static shared memory would not fit a dynamic
+    // block just under the 48 KB default.
+    int optin = 0;
+    SPGX_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    const int cap = optin - 256;
+    if (tile_smem > size_t(cap)) {
+        set_error("a tile needs more shared memory than the device offers; lower tile_vertices");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    {
+        auto raise = [cap](const void *fn) -> cudaError_t {
+            return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
         };
         SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<1>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<2>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<4>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<8>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<1>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<2>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<4>)));
+        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<8>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<1>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<2>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<4>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<8>)));
     }
+    return SPGX_OK;
+}
+
+// Dataflow tables: each tile's colour and its neighbour tiles (the owners of its halo
+// vertices, and itself), the per-tile sweep counters and the resident CTAs per SM.
+spgx_status VbdSolver::setup_flow()
+{
+    const int n_tiles = TL.color_tiles.empty() ? 0 : TL.color_tiles.back();
+    std::vector<int32_t> color(std::max(1, n_tiles), 0), tile_of(std::max(1, L.nv), -1);
+    for (int c = 0; c < L.n_colors; ++c)
+        for (int t = TL.color_tiles[c]; t < TL.color_tiles[c + 1]; ++t) {
+            color[t] = c;
+            const I4 h = TL.hdr[2 * t];
+            for (int i = 0; i < h.y; ++i) tile_of[h.x + i] = t;
+        }
+    std::vector<int32_t> off(n_tiles + 1, 0), nbr;
+    std::vector<int32_t> tmp;
+    for (int t = 0; t < n_tiles; ++t) {
+        const I4 h = TL.hdr[2 * t];
+        tmp.assign(1, t);
+        for (int i = 0; i < h.w; ++i) tmp.push_back(tile_of[TL.halo[h.z + i]]);
+        std::sort(tmp.begin(), tmp.end());
+        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+        if (!tmp.empty() && tmp.front() < 0) {
+            set_error("internal: a halo vertex belongs to no tile");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        nbr.insert(nbr.end(), tmp.begin(), tmp.end());
+        off[t + 1] = static_cast<int32_t>(nbr.size());
+    }
+    if (nbr.empty()) nbr.push_back(0);
+    SPGX_TRY_STATUS(fl_nbr_off.upload(off));
+    SPGX_TRY_STATUS(fl_nbr.upload(nbr));
+    SPGX_TRY_STATUS(fl_color.upload(color));
+    SPGX_TRY_STATUS(fl_epoch.alloc(size_t(std::max(1, n_tiles)) * sizeof(int)));
+    SPGX_TRY_STATUS(fl_ticket.alloc(2 * sizeof(int)));
+    FV = FlowView{fl_nbr_off.as<int>(), fl_nbr.as<int>(), fl_color.as<int>(), fl_epoch.as<int>(), fl_ticket.as<int>()};
+    SPGX_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
+    const int T = TL.tile_vertices;
+    const void *fns[4] = {reinterpret_cast<const void *>(vbd_flow_kernel<1>),
+                          reinterpret_cast<const void *>(vbd_flow_kernel<2>),
+                          reinterpret_cast<const void *>(vbd_flow_kernel<4>),
+                          reinterpret_cast<const void *>(vbd_flow_kernel<8>)};
+    const int gs[4] = {1, 2, 4, 8};
+    for (int i = 0; i < 4; ++i) {
+        flow_blocks_per_sm[i] = 0;
+        if (T * gs[i] > kTileThreads) continue;
+        SPGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&flow_blocks_per_sm[i], fns[i], T * gs[i], tile_smem));
+    }
+    return reset_flow();
+}
+
+spgx_status VbdSolver::take_flow_launch_error()
+{
+    const cudaError_t e = flow_launch_error;
+    flow_launch_error = cudaSuccess;
+    if (e == cudaSuccess) return SPGX_OK;
+    set_error(std::string("dataflow kernel launch: ") + cudaGetErrorString(e));
+    return SPGX_ERR_CUDA;
+}
+
+spgx_status VbdSolver::reset_flow()
+{
+    const int n_tiles = TL.color_tiles.empty() ? 0 : TL.color_tiles.back();
+    SPGX_CUDA(cudaMemsetAsync(fl_epoch.as<int>(), 0, size_t(std::max(1, n_tiles)) * sizeof(int), stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    flow_epoch = 0;
     return SPGX_OK;
 }
 
@@ -457,8 +667,8 @@ spgx_status VbdSolver::check_params(const spgx_vbd_params *p)
         set_error("lanes_per_vertex must be 0, 1, 2, 4, 8, 16 or 32");
         return SPGX_ERR_INVALID_ARG;
     }
-    if (p->kernel < 0 || p->kernel > 2 || p->tile_vertices < 0 || p->tile_vertices > kTileMaxVerts) {
-        set_error("kernel must be 0, 1 or 2 and tile_vertices in [0, 128]");
+    if (p->kernel < 0 || p->kernel > 3 || p->tile_vertices < 0 || p->tile_vertices > kTileMaxVerts) {
+        set_error("kernel must be 0, 1, 2 or 3 and tile_vertices in [0, 128]");
         return SPGX_ERR_INVALID_ARG;
     }
     if (p->block_size != 0 && (p->block_size % 32 != 0 || p->block_size < 32 || p->block_size > 256)) {
@@ -501,6 +711,7 @@ spgx_status VbdSolver::configure_launch()
     std::vector<Cand> cands;
     const bool want_lanes = P.kernel == 0 || P.kernel == 1;
     const bool want_tiles = P.kernel == 0 || P.kernel == 2;
+    const bool want_flow = P.kernel == 0 || P.kernel == 3;
     std::vector<int> blocks;
     if (P.block_size)
         blocks.push_back(P.block_size);
@@ -520,6 +731,17 @@ spgx_status VbdSolver::configure_launch()
         for (int g : {1, 2, 4, 8})
             if (TL.tile_vertices * g <= kTileThreads && (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
                 cands.push_back({2, g, TL.tile_vertices * g});
+    if (want_flow)
+        for (int g : {1, 2, 4, 8}) {
+            const int li = g == 1 ? 0 : g == 2 ? 1 : g == 4 ? 2 : 3;
+            if (TL.tile_vertices * g <= kTileThreads && TL.tile_vertices * g >= 32 && flow_blocks_per_sm[li] > 0 &&
+                (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
+                cands.push_back({3, g, TL.tile_vertices * g});
+        }
+    if (cands.empty()) {
+        set_error("no kernel variant fits the requested launch parameters");
+        return SPGX_ERR_INVALID_ARG;
+    }
     if (cands.size() == 1 || L.nv == 0) {
         kernel = cands[0].kernel;
         lanes = cands[0].lanes;
@@ -549,9 +771,17 @@ spgx_status VbdSolver::configure_launch()
         SPGX_CUDA(cudaMemcpyAsync(S.pos, d_backup.as<void>(), size_t(L.nv) * 2 * sizeof(float4),
                                   cudaMemcpyDeviceToDevice, stream));
     }
-    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, 4 * sizeof(int), stream));
+    int *hc = h_counters.as<int>();
+    SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), kCounters * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, kCounters * sizeof(int), stream));
     SPGX_CUDA(cudaStreamSynchronize(stream));
     SPGX_CUDA(cudaGetLastError());
+    SPGX_TRY_STATUS(take_flow_launch_error());
+    if (hc[2] & 2u) {
+        SPGX_TRY_STATUS(reset_flow());
+        set_error("a dataflow sweep gave up waiting for a neighbour tile while timing launch shapes");
+        return SPGX_ERR_TIMEOUT;
+    }
     kernel = pick.kernel;
     lanes = pick.lanes;
     block = pick.block;
@@ -568,7 +798,7 @@ spgx_status VbdSolver::build_graph()
     SPGX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     for (int s = 0; s < P.substeps; ++s) {
         launch_begin(*this, stream);
-        if (W.enabled) launch_warm(stream);
+        if (W.mode != kWarmInertial) launch_warm(stream);
         launch_iterations(*this, P.iterations, stream);
         launch_end(*this, stream);
     }
@@ -592,6 +822,18 @@ spgx_status VbdSolver::profile_sweeps(int iterations, double *color_ms)
     SPGX_TRY_STATUS(X.upload_if_dirty(stream));
     X.mark_device_advanced();
     const int nc = L.n_colors;
+    if (kernel == 3) {  // no per-colour launches: the whole sweep goes to color_ms[0]
+        SPGX_CUDA(cudaEventRecord(ev0, stream));
+        launch_iterations(*this, iterations, stream);
+        SPGX_CUDA(cudaEventRecord(ev1, stream));
+        SPGX_CUDA(cudaGetLastError());
+        SPGX_CUDA(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        for (int c = 0; c < nc; ++c) color_ms[c] = 0.0;
+        if (nc > 0) color_ms[0] = ms / std::max(1, iterations);
+        return SPGX_OK;
+    }
     std::vector<cudaEvent_t> ev(size_t(nc) * iterations * 2, nullptr);
     for (auto &e : ev) SPGX_CUDA(cudaEventCreate(&e));
     for (int it = 0; it < iterations; ++it)
@@ -620,26 +862,32 @@ spgx_status VbdSolver::residual_norm(double *out)
     SPGX_CUDA(cudaMemsetAsync(d_resid.as<double>(), 0, sizeof(double), stream));
     launch_residual(*this, stream);
     SPGX_CUDA(cudaGetLastError());
-    double *hr = reinterpret_cast<double *>(h_counters.as<int>() + 4);
+    double *hr = reinterpret_cast<double *>(h_counters.as<int>() + kCounters);
     SPGX_CUDA(cudaMemcpyAsync(hr, d_resid.as<double>(), sizeof(double), cudaMemcpyDeviceToHost, stream));
     SPGX_CUDA(cudaStreamSynchronize(stream));
     *out = std::sqrt(*hr);
     return SPGX_OK;
 }
 
-// Learned initial guess of one substep, after the inertial predict (all on the stream, no host
-// round trip): wres[0] = ||r(y)||^2, the MLP's candidate x_w = y + l * MLP(features),
-// wres[1] = ||r(x_w)||^2, and x_w is kept only when its residual is lower.
+// Initial guess of one substep, after the inertial predict, all on the stream with no host
+// round trip. wres[0] = ||r(y)||^2. Extrapolated mode: wres[1] = ||r(x_e)||^2. Learned mode:
+// wres[2] = ||r(x_e)||^2 and wres[1] = ||r(x_e + l MLP)||^2. The substep then starts from the
+// guess with the lowest residual, so the network can only help.
 void VbdSolver::launch_warm(cudaStream_t st)
 {
     double *wres = W.wres.as<double>();
-    cudaMemsetAsync(wres, 0, 2 * sizeof(double), st);
+    cudaMemsetAsync(wres, 0, 3 * sizeof(double), st);
     launch_residual(*this, st, wres);
-    launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, st);
-    W.mlp->infer(W.feats.as<float>(), L.nv, W.out.as<float>(), st);
-    launch_warm_apply(W, X.pos(), X.tgt(), L.nv, h_sub, st);
-    launch_residual(*this, st, wres + 1);
-    launch_warm_select(W, X.pos(), X.tgt(), L.nv, d_counters.as<int>() + 3, st);
+    const bool learned = W.mode == kWarmLearned;
+    launch_warm_extrapolate(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, st);
+    launch_residual(*this, st, wres + (learned ? 2 : 1));
+    if (learned) {
+        launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, st);
+        W.mlp->infer(W.feats.as<float>(), L.nv, W.out.as<float>(), st);
+        launch_warm_apply(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, st);
+        launch_residual(*this, st, wres + 1);
+    }
+    launch_warm_select(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, learned, d_counters.as<int>(), st);
 }
 
 // Uploads positions/velocities set from the host; a replaced state restarts the displacement
@@ -668,7 +916,7 @@ spgx_status VbdSolver::enable_history()
     SPGX_TRY_STATUS(W.vhist.alloc(n * sizeof(float4)));
     SPGX_TRY_STATUS(W.feats.alloc(n * kWarmFeatures * sizeof(float)));
     SPGX_TRY_STATUS(W.out.alloc(n * 3 * sizeof(float)));
-    SPGX_TRY_STATUS(W.wres.alloc(2 * sizeof(double)));
+    SPGX_TRY_STATUS(W.wres.alloc(3 * sizeof(double)));
     // No earlier motion is known: take the previous step's displacement equal to the current
     // velocity's (constant-velocity history).
     SPGX_TRY_STATUS(X.upload_if_dirty(stream));
@@ -680,10 +928,14 @@ spgx_status VbdSolver::enable_history()
     return SPGX_OK;
 }
 
-spgx_status VbdSolver::set_warm_start(const Mlp *mlp, bool enable)
+spgx_status VbdSolver::set_warm_start(const Mlp *mlp, int mode)
 {
-    if (enable && !mlp) {
-        set_error("enabling the warm start needs an MLP handle");
+    if (mode < kWarmInertial || mode > kWarmExtrapolate) {
+        set_error("warm-start mode must be 0 (inertial), 1 (learned) or 2 (extrapolated)");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (mode == kWarmLearned && !mlp) {
+        set_error("the learned warm start needs an MLP handle");
         return SPGX_ERR_INVALID_ARG;
     }
     if (mlp && mlp->device != device) {
@@ -692,7 +944,7 @@ spgx_status VbdSolver::set_warm_start(const Mlp *mlp, bool enable)
     }
     SPGX_TRY_STATUS(enable_history());
     W.mlp = mlp;
-    W.enabled = enable;
+    W.mode = mode;
     graph_valid = false;
     return SPGX_OK;
 }
@@ -706,18 +958,19 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
     }
     SPGX_TRY_STATUS(upload_state());
     X.mark_device_advanced();
+    if (flow_epoch > (1 << 30)) SPGX_TRY_STATUS(reset_flow());  // keep the sweep counters far from overflow
     spgx_step_stats st{};
-    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, 4 * sizeof(int), stream));
+    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, kCounters * sizeof(int), stream));
     SPGX_CUDA(cudaEventRecord(ev0, stream));
-    double *hw = reinterpret_cast<double *>(h_counters.as<int>() + 4);  // 2 doubles of pinned scratch
+    double *hw = reinterpret_cast<double *>(h_counters.as<int>() + kCounters);  // 4 doubles of pinned scratch
     if (P.tolerance <= 0 && !record) {
-        if (P.use_graph) {
+        if (P.use_graph && kernel != 3) {
             if (!graph_valid) SPGX_TRY_STATUS(build_graph());
             SPGX_CUDA(cudaGraphLaunch(graph_exec, stream));
         } else {
             for (int s = 0; s < P.substeps; ++s) {
                 launch_begin(*this, stream);
-                if (W.enabled) launch_warm(stream);
+                if (W.mode != kWarmInertial) launch_warm(stream);
                 launch_iterations(*this, P.iterations, stream);
                 launch_end(*this, stream);
             }
@@ -729,19 +982,23 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
         for (int s = 0; s < P.substeps; ++s) {
             launch_begin(*this, stream);
             double r0 = 0, r = 0;
-            if (W.enabled) {
+            if (W.mode != kWarmInertial) {
                 launch_warm(stream);
-                SPGX_CUDA(cudaMemcpyAsync(hw, W.wres.as<double>(), 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                SPGX_CUDA(cudaMemcpyAsync(hw, W.wres.as<double>(), 3 * sizeof(double), cudaMemcpyDeviceToHost,
                                           stream));
                 SPGX_CUDA(cudaStreamSynchronize(stream));
+                const bool learned = W.mode == kWarmLearned;
                 r0 = std::sqrt(hw[0]);
                 st.residual_warm = std::sqrt(hw[1]);
-                r = hw[1] < hw[0] ? st.residual_warm : r0;
+                st.residual_extrapolated = std::sqrt(learned ? hw[2] : hw[1]);
+                r = std::sqrt(std::min(hw[0], std::min(hw[1], learned ? hw[2] : hw[1])));
             } else {
-                if (record) launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, stream);
                 if (P.tolerance > 0) SPGX_TRY_STATUS(residual_norm(&r0));
                 r = r0;
             }
+            // Features depend on the velocities and the history only; the learned guess has
+            // computed them already.
+            if (record && W.mode != kWarmLearned) launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, stream);
             if (P.tolerance > 0) {
                 int it = 0;
                 while (it < P.max_iterations && r > P.tolerance * r0) {
@@ -764,8 +1021,9 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
     }
     SPGX_CUDA(cudaEventRecord(ev1, stream));
     SPGX_CUDA(cudaGetLastError());
+    SPGX_TRY_STATUS(take_flow_launch_error());
     int *hc = h_counters.as<int>();
-    SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), kCounters * sizeof(int), cudaMemcpyDeviceToHost, stream));
     if (features)
         SPGX_CUDA(cudaMemcpyAsync(features, W.feats.as<float>(), size_t(L.nv) * kWarmFeatures * sizeof(float),
                                   cudaMemcpyDeviceToHost, stream));
@@ -779,7 +1037,13 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
     st.fallback_solves = hc[0];
     st.skipped_solves = hc[1];
     st.warm_accepted = hc[3];
+    st.extrapolated_accepted = hc[4];
     if (stats) *stats = st;
+    if (hc[2] & 2u) {
+        SPGX_TRY_STATUS(reset_flow());
+        set_error("a dataflow sweep gave up waiting for a neighbour tile; the step is incomplete");
+        return SPGX_ERR_TIMEOUT;
+    }
     if (hc[2] & 1u) {
         set_error("a vertex update produced a non-finite position; the update was not stored");
         return SPGX_ERR_NONFINITE;
@@ -904,15 +1168,11 @@ spgx_status spgx_vbd_residual(spgx_vbd *h, double *norm)
     SPGX_GUARD_END
 }
 
-spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t enable)
+spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t mode)
 {
     SPGX_GUARD_BEGIN
     SPGX_HANDLE(h);
-    if (enable != 0 && enable != 1) {
-        spgx::set_error("enable must be 0 or 1");
-        return SPGX_ERR_INVALID_ARG;
-    }
-    return h->s->set_warm_start(mlp ? mlp->m.get() : nullptr, enable == 1);
+    return h->s->set_warm_start(mlp ? mlp->m.get() : nullptr, mode);
     SPGX_GUARD_END
 }
 

@@ -24,7 +24,7 @@ struct VbdSolver {
     spgx_vbd_params P{};
     double h_sub{0.01};
     int device{0};
-    int kernel{1};  // 1: lanes-per-vertex kernel, 2: shared-memory tile kernel
+    int kernel{1};  // 1: lanes-per-vertex kernel, 2: shared-memory tile kernel, 3: dataflow tiles
     int lanes{1};
     int block{128};
     cudaStream_t stream{nullptr};
@@ -42,6 +42,12 @@ struct VbdSolver {
     DevBuf tb_hdr, tb_halo, tb_records, tb_vrec;
     TileView TV{};
     size_t tile_smem{0};
+    DevBuf fl_nbr_off, fl_nbr, fl_color, fl_epoch, fl_ticket;
+    FlowView FV{};
+    int flow_blocks_per_sm[4]{};  // per lanes variant 1, 2, 4, 8
+    int num_sms{0};
+    mutable int flow_epoch{0};    // sweeps the dataflow kernel has completed on this handle
+    mutable cudaError_t flow_launch_error{cudaSuccess};
     WarmStart W;
 
     VbdSolver() = default;
@@ -54,6 +60,9 @@ struct VbdSolver {
     spgx_status set_params(const spgx_vbd_params *params);
     spgx_status configure_launch();
     spgx_status setup_tiles();
+    spgx_status setup_flow();
+    spgx_status reset_flow();
+    spgx_status take_flow_launch_error();
     spgx_status build_graph();
     spgx_status residual_norm(double *out);
     spgx_status profile_sweeps(int iterations, double *color_ms);
@@ -62,7 +71,7 @@ struct VbdSolver {
     spgx_status step(spgx_step_stats *stats, float *features = nullptr, float *targets = nullptr);
     spgx_status enable_history();
     spgx_status upload_state();
-    spgx_status set_warm_start(const Mlp *mlp, bool enable);
+    spgx_status set_warm_start(const Mlp *mlp, int mode);
     void launch_warm(cudaStream_t st);
 };
 

@@ -24,6 +24,15 @@ struct TileView {
     const int *vrec;      // per internal vertex: record offset inside its tile's block
 };
 
+// Tables of the dataflow kernel (vbd_flow_kernel).
+struct FlowView {
+    const int *nbr_off;     // per tile: range in nbr
+    const int *nbr;         // neighbour tiles (self included)
+    const int *tile_color;  // colour of each tile
+    int *epoch;             // per tile: sweeps completed (monotonic over launches)
+    int *ticket;            // [0] next task, [1] abort flag (both zeroed before a launch)
+};
+
 inline size_t tile_smem_bytes(int max_local, int max_records)
 {
     return size_t(2 * max_local) * 16 + size_t(max_records) * 16;

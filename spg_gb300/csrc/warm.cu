@@ -112,25 +112,60 @@ __global__ void warm_features_kernel(const float4 *__restrict__ vel, const float
     f[23] = 1.f;
 }
 
+// x_e - base = (y - base) + h (v_n - v_{n-1}) - h^2 g: the last step's acceleration carried
+// over (x_e = x_n + 2 (x_n - x_{n-1}) - (x_{n-1} - x_{n-2})). vel holds v_n + h g here.
+__device__ __forceinline__ float3 extrapolated_delta(float4 t, float4 v, float4 p, float h, float ghx, float ghy,
+                                                     float ghz)
+{
+    return make_float3(t.x + h * (v.x - p.x - 2.f * ghx), t.y + h * (v.y - p.y - 2.f * ghy),
+                       t.z + h * (v.z - p.z - 2.f * ghz));
+}
+
+// The learned guess: the extrapolated one plus l times the network's correction.
 __global__ void warm_apply_kernel(float4 *__restrict__ pos, const float4 *__restrict__ tgt,
-                                  const float *__restrict__ out, int nv, float ell)
+                                  const float4 *__restrict__ vel, const float4 *__restrict__ vhist,
+                                  const float *__restrict__ out, int nv, float h, float ghx, float ghy, float ghz,
+                                  float ell)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
-    const float4 t = tgt[i];
+    const float3 e = extrapolated_delta(tgt[i], vel[i], vhist[i], h, ghx, ghy, ghz);
     const float *o = out + size_t(i) * 3;
-    pos[2 * i + 1] = make_float4(t.x + ell * o[0], t.y + ell * o[1], t.z + ell * o[2], 0.f);
+    pos[2 * i + 1] = make_float4(e.x + ell * o[0], e.y + ell * o[1], e.z + ell * o[2], 0.f);
 }
 
-__global__ void warm_select_kernel(float4 *__restrict__ pos, const float4 *__restrict__ tgt,
-                                   const double *__restrict__ wres, int nv, int *accepted)
+__global__ void warm_extrapolate_kernel(float4 *__restrict__ pos, const float4 *__restrict__ tgt,
+                                        const float4 *__restrict__ vel, const float4 *__restrict__ vhist, int nv,
+                                        float h, float ghx, float ghy, float ghz)
 {
-    const bool keep = wres[1] < wres[0];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0 && keep) atomicAdd(accepted, 1);
+    if (i >= nv) return;
+    const float3 e = extrapolated_delta(tgt[i], vel[i], vhist[i], h, ghx, ghy, ghz);
+    pos[2 * i + 1] = make_float4(e.x, e.y, e.z, 0.f);
+}
+
+// Chooses the start of the substep by residual. The positions hold the candidate whose squared
+// residual is wres[1] (the learned guess with three_way, else the extrapolated one); wres[0]
+// is y's and, with three_way, wres[2] the extrapolated guess's. Ties keep the simpler guess.
+__global__ void warm_select_kernel(float4 *__restrict__ pos, const float4 *__restrict__ tgt,
+                                   const float4 *__restrict__ vel, const float4 *__restrict__ vhist,
+                                   const double *__restrict__ wres, int nv, bool three_way, float h, float ghx,
+                                   float ghy, float ghz, int *counters)
+{
+    const double r0 = wres[0], r1 = wres[1], r2 = three_way ? wres[2] : INFINITY;
+    const bool keep = r1 < r0 && r1 < r2;
+    const bool extrap = !keep && r2 < r0;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && keep) atomicAdd(counters + (three_way ? 3 : 4), 1);
+    if (i == 0 && extrap) atomicAdd(counters + 4, 1);
     if (keep || i >= nv) return;
     const float4 t = tgt[i];
-    pos[2 * i + 1] = make_float4(t.x, t.y, t.z, 0.f);
+    if (extrap) {
+        const float3 e = extrapolated_delta(t, vel[i], vhist[i], h, ghx, ghy, ghz);
+        pos[2 * i + 1] = make_float4(e.x, e.y, e.z, 0.f);
+    } else {
+        pos[2 * i + 1] = make_float4(t.x, t.y, t.z, 0.f);
+    }
 }
 
 __global__ void warm_targets_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ tgt, int nv,
@@ -156,16 +191,30 @@ void launch_warm_features(const WarmStart &W, const float4 *vel, int nv, double 
         float(g[2] / kWarmG0), W.feats.as<float>());
 }
 
-void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, int nv, double h, cudaStream_t st)
+void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
+                       const double *g, cudaStream_t st)
 {
     if (nv == 0) return;
-    warm_apply_kernel<<<grid_for(nv), 256, 0, st>>>(pos, tgt, W.out.as<float>(), nv, float(h * h * kWarmG0));
+    warm_apply_kernel<<<grid_for(nv), 256, 0, st>>>(pos, tgt, vel, W.vhist.as<float4>(), W.out.as<float>(), nv,
+                                                    float(h), float(h * g[0]), float(h * g[1]), float(h * g[2]),
+                                                    float(h * h * kWarmG0));
 }
 
-void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, int nv, int *accepted, cudaStream_t st)
+void launch_warm_extrapolate(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
+                             const double *g, cudaStream_t st)
 {
     if (nv == 0) return;
-    warm_select_kernel<<<grid_for(nv), 256, 0, st>>>(pos, tgt, W.wres.as<double>(), nv, accepted);
+    warm_extrapolate_kernel<<<grid_for(nv), 256, 0, st>>>(pos, tgt, vel, W.vhist.as<float4>(), nv, float(h),
+                                                          float(h * g[0]), float(h * g[1]), float(h * g[2]));
+}
+
+void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
+                        const double *g, bool three_way, int *counters, cudaStream_t st)
+{
+    if (nv == 0) return;
+    warm_select_kernel<<<grid_for(nv), 256, 0, st>>>(pos, tgt, vel, W.vhist.as<float4>(), W.wres.as<double>(), nv,
+                                                     three_way, float(h), float(h * g[0]), float(h * g[1]),
+                                                     float(h * g[2]), counters);
 }
 
 void launch_warm_targets(const float4 *pos, const float4 *tgt, int nv, double h, float *targets, cudaStream_t st)

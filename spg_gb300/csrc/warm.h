@@ -12,7 +12,10 @@
 //   20   one-ring size / 8 21   |d1| / l         22    |lap(d1)| / l     23  1
 // The one-ring is every vertex sharing a mesh edge, a triangle or a tet with i (the two
 // opposite vertices of a bending stencil are not neighbours of each other).
-// Target and output: (x* - y) / l, the converged position's offset from the inertial guess.
+// Recorded target: (x* - y) / l, the converged position's offset from the inertial guess.
+// Network output: the correction c to the extrapolated guess, x_w = x_n + 2 d1 - d2 + l c
+// (the last step's acceleration carried over, plus the learned remainder), so the network is
+// trained on (x* - y) / l - (d1 - d2 - h^2 g) / l = target - (f[3:6] - f[6:9] - f[15:18]).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,20 +37,29 @@ struct Mlp;
 void build_vertex_neighbours(const SceneLayout &L, std::vector<int32_t> &off, std::vector<int32_t> &nbr,
                              std::vector<F4> &stat);
 
+// Initial-guess modes of spgx_vbd_set_warm_start.
+enum WarmMode { kWarmInertial = 0, kWarmLearned = 1, kWarmExtrapolate = 2 };
+
 struct WarmStart {
     bool history{false};  // history buffers exist and are maintained every substep
-    bool enabled{false};  // the learned guess is tried at the start of every substep
+    int mode{kWarmInertial};
     const Mlp *mlp{nullptr};
     DevBuf nbr_off, nbr, stat, vhist, feats, out, wres;
 };
 
 // feats = features of every vertex at the start of the substep (after the inertial predict).
 void launch_warm_features(const WarmStart &W, const float4 *vel, int nv, double h, const double *g, cudaStream_t st);
-// delta = tgt + l * out for every vertex (the candidate guess).
-void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, int nv, double h, cudaStream_t st);
-// Keeps the candidate when wres[1] < wres[0] (squared residual norms at the candidate and at
-// y), else restores delta = tgt; adds 1 to *accepted when kept.
-void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, int nv, int *accepted, cudaStream_t st);
+// delta = tgt + h (v_n - v_{n-1}) - h^2 g + l * out for every vertex (the learned guess).
+void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
+                       const double *g, cudaStream_t st);
+// delta = tgt + h (v_n - v_{n-1}) - h^2 g (the previous step's acceleration carried over).
+void launch_warm_extrapolate(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
+                             const double *g, cudaStream_t st);
+// Starts the substep from the guess with the lowest residual: the candidate in the positions
+// (squared residual wres[1]), y (wres[0]) or, with three_way, the extrapolated guess
+// (wres[2]). Counts the pick in counters[3] (learned) or counters[4] (extrapolated).
+void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
+                        const double *g, bool three_way, int *counters, cudaStream_t st);
 // targets = (x - y) / l for every vertex (training data of the converged step).
 void launch_warm_targets(const float4 *pos, const float4 *tgt, int nv, double h, float *targets, cudaStream_t st);
 

@@ -58,8 +58,8 @@ class XpbdParams(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("fallback_solves", C.c_int32), ("skipped_solves", C.c_int32),
                 ("converged", C.c_int32), ("residual_initial", C.c_double), ("residual_final", C.c_double),
-                ("device_ms", C.c_double), ("warm_accepted", C.c_int32), ("reserved0", C.c_int32),
-                ("residual_warm", C.c_double)]
+                ("device_ms", C.c_double), ("warm_accepted", C.c_int32), ("extrapolated_accepted", C.c_int32),
+                ("residual_warm", C.c_double), ("residual_extrapolated", C.c_double)]
 
 
 _lib = None
@@ -254,11 +254,13 @@ class VbdSolver:
         check(lib().spgx_vbd_profile_sweeps(self.h, iterations, _p(out, C.c_double)))
         return out
 
-    def set_warm_start(self, mlp=None, enable=True):
-        """Attaches `mlp` (an Mlp) as the learned initial guess; also starts the displacement
-        history. enable=False keeps the history but uses the inertial guess."""
+    def set_warm_start(self, mlp=None, mode=None):
+        """Initial guess of every substep: mode 0 inertial (history kept), 1 learned (`mlp`, an
+        Mlp), 2 extrapolated acceleration. Default: 1 with an mlp, else 0."""
+        if mode is None:
+            mode = 0 if mlp is None else 1
         self._mlp = mlp
-        check(lib().spgx_vbd_set_warm_start(self.h, None if mlp is None else mlp.h, 1 if enable else 0))
+        check(lib().spgx_vbd_set_warm_start(self.h, None if mlp is None else mlp.h, int(mode)))
 
     def step_record(self):
         """One step returning (stats, features [n x 24], targets [n x 3]) in internal vertex order."""

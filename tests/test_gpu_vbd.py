@@ -68,7 +68,7 @@ def test_element_blocks_match_tinyad_fp64(scene):
         assert np.quantile(eh, 0.99) <= 1e-5
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 def test_cloth_cfg1_positions_after_10_steps(kernel):
     """33x33 StVK cloth, 100 iterations/step, 10 steps: |x_gpu - x_fp64| <= 1e-4 extent."""
     obj = scenes.cloth_cfg1()
@@ -85,7 +85,7 @@ def test_cloth_cfg1_positions_after_10_steps(kernel):
     assert err <= 1e-4 * extent
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 def test_spring_cloth_positions_after_10_steps(kernel):
     obj = scenes.spring_cloth_cfg3(65)
     gpu = N.VbdSolver([obj], dt=1 / 120, iterations=20, gravity=scenes.GRAVITY, kernel=kernel)
@@ -101,7 +101,7 @@ def test_spring_cloth_positions_after_10_steps(kernel):
     assert err <= 1e-4 * extent
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 def test_snh_beam_positions(kernel):
     obj = scenes.beam_cfg2(11, 4, 4)
     gpu = N.VbdSolver([obj], dt=1 / 60, iterations=50, gravity=scenes.GRAVITY, kernel=kernel)
@@ -117,7 +117,7 @@ def test_snh_beam_positions(kernel):
     assert err <= 1e-4 * extent
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 def test_batch_matches_independent_solvers(kernel):
     objs = scenes.patch_batch_cfg4(6, 8, 20, seed=3)
     gpu = N.VbdSolver(objs, dt=1 / 60, iterations=30, gravity=scenes.GRAVITY, kernel=kernel)
@@ -132,7 +132,7 @@ def test_batch_matches_independent_solvers(kernel):
         assert np.abs(xg - xr).max() <= 1e-4
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 def test_residual_matches_oracle(kernel):
     """FP64-reduced residual ||M/h^2 (x - y) + grad E(x)|| of the GPU state against the
     oracle's at the same state and inertial target."""
@@ -162,3 +162,25 @@ def test_colors_and_adjacency_through_handle():
     c1, e1 = gpu.adjacency(0)
     c2, e2 = ref.adjacency(len(obj.energies))
     assert np.array_equal(c1, c2) and np.array_equal(e1, e2)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_dataflow_kernel_equals_colour_launches(lanes):
+    """The dataflow kernel runs the same Gauss-Seidel order as one launch per colour, so with
+    the same lanes per vertex (same per-vertex summation order) it gives the same positions
+    bit for bit, over steps of 20 sweeps and for a tolerance-mode step."""
+    from spg_gb300 import scenes as S
+    obj = S.spring_cloth(129).objects[0]
+    kw = dict(dt=1 / 120, iterations=20, gravity=scenes.GRAVITY, lanes_per_vertex=lanes)
+    a = N.VbdSolver([obj], kernel=2, **kw)
+    b = N.VbdSolver([obj], kernel=3, **kw)
+    assert a.launch() == (2, lanes, 64 * lanes) and b.launch() == (3, lanes, 64 * lanes)
+    for _ in range(3):
+        a.step()
+        b.step()
+    assert np.array_equal(a.state(0)[0], b.state(0)[0])
+    a.set_params(tolerance=1e-4, max_iterations=400, check_interval=50)
+    b.set_params(tolerance=1e-4, max_iterations=400, check_interval=50)
+    sa, sb = a.step(), b.step()
+    assert sa.iterations == sb.iterations
+    assert np.array_equal(a.state(0)[0], b.state(0)[0])

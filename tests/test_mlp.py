@@ -125,20 +125,43 @@ def _patch(n=17):
 
 
 @pytest.mark.gpu
-def test_zero_network_is_rejected_and_changes_nothing():
-    """A zero network proposes x_w = y, whose residual is not lower: every guess is rejected
-    and the trajectory equals the plain solver's bit for bit."""
+def test_zero_network_equals_the_extrapolated_guess():
+    """The network only corrects the extrapolated guess: with zero weights the learned mode
+    proposes exactly that guess, so its trajectory equals mode 2's bit for bit."""
     obj = _patch()
     kw = dict(dt=1 / 120, iterations=10, gravity=(0, 0, -9.81))
-    plain = N.VbdSolver([obj], **kw)
+    ext = N.VbdSolver([obj], **kw)
+    ext.set_warm_start(None, mode=2)
     warm = N.VbdSolver([obj], **kw)
     mlp = N.Mlp(seed=0, weights=np.zeros(M.N_PARAMS, np.float32))
     warm.set_warm_start(mlp)
     for _ in range(4):
-        plain.step()
+        a = ext.step()
+        b = warm.step()
+        assert b.warm_accepted == 0  # ties keep the simpler guess
+        assert a.extrapolated_accepted == b.extrapolated_accepted
+    assert np.array_equal(ext.state(0)[0], warm.state(0)[0])
+
+
+@pytest.mark.gpu
+def test_worse_learned_guess_is_never_used():
+    """A network whose correction is huge makes a guess with a larger residual than both y and
+    the extrapolated guess: it is never picked, and the trajectory equals mode 2's bit for bit."""
+    obj = _patch()
+    kw = dict(dt=1 / 120, iterations=10, gravity=(0, 0, -9.81))
+    ext = N.VbdSolver([obj], **kw)
+    ext.set_warm_start(None, mode=2)
+    warm = N.VbdSolver([obj], **kw)
+    w = np.zeros(M.N_PARAMS, np.float32)
+    w[M.N_PARAMS - 3:] = 1e4   # b4: a constant correction of 1e4 l (about 7 m) per vertex
+    mlp = N.Mlp(seed=0, weights=w)
+    warm.set_warm_start(mlp)
+    for _ in range(4):
+        a = ext.step()
         st = warm.step()
         assert st.warm_accepted == 0
-    assert np.array_equal(plain.state(0)[0], warm.state(0)[0])
+        assert st.extrapolated_accepted == a.extrapolated_accepted
+    assert np.array_equal(ext.state(0)[0], warm.state(0)[0])
 
 
 @pytest.mark.gpu
@@ -148,7 +171,7 @@ def test_recorded_features_and_targets():
     obj = _patch()
     h, g = 1 / 120, np.array([0.0, 0.0, -9.81])
     s = N.VbdSolver([obj], dt=h, iterations=10, gravity=tuple(g))
-    s.set_warm_start(None, enable=False)
+    s.set_warm_start(None, mode=0)
     xs = [s.state(0)[0]]
     for _ in range(3):
         s.step()
