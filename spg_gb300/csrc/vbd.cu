@@ -28,9 +28,8 @@ namespace spgx {
 // det(H) > 1e-10. The solve runs in FP32 on the max-norm-scaled block unless its Frobenius
 // condition estimate exceeds the fallback threshold, in which case it is redone in FP64.
 __device__ __forceinline__ void solve_and_update(const DevState &S, int v, const Block<float> &acc, float4 d4,
-                                                 float invdt2, float fb2)
+                                                 float4 tg, float invdt2, float fb2)
 {
-    const float4 tg = S.tgt[v];
     const float c = tg.w * invdt2;
     const float f0 = acc.f[0] - c * (d4.x - tg.x);
     const float f1 = acc.f[1] - c * (d4.y - tg.y);
@@ -108,7 +107,7 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
     accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
     group_reduce<G>(acc);
     allow_next_grid();
-    if (active && lane == 0) solve_and_update(S, v, acc, S.pos[2 * v + 1], invdt2, fb2);
+    if (active && lane == 0) solve_and_update(S, v, acc, S.pos[2 * v + 1], S.tgt[v], invdt2, fb2);
 }
 
 // One colour phase with the shared-memory tile kernel: one CTA per tile of the colour,
@@ -121,25 +120,22 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
     float4 *sb = dyn;
     float4 *sd = dyn + max_local;
     int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
-    const int4 h0 = tile_stage(V, S.pos, tile0 + blockIdx.x, sb, sd, srec);
+    TileVertex tv;
+    const int4 h0 = tile_stage<G>(V, S, tile0 + blockIdx.x, sb, sd, srec, tv);
     const int lv = threadIdx.x / G;
     const int lane = threadIdx.x & (G - 1);
     const bool active = lv < h0.y;
-    int4 hv = make_int4(0, 0, 0, 0);
-    int roff = 0;
     TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
     if (active) {
-        hv = __ldg(S.hdr + h0.x + lv);
-        roff = __ldg(V.vrec + h0.x + lv);
         cx.bs = v3(sb[lv]);
         cx.ds = v3(sd[lv]);
     }
     Block<float> acc;
     block_zero(acc);
-    tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+    tile_vertex_accumulate<G>(cx, tv.hv, tv.roff, lane, acc);
     group_reduce<G>(acc);
     allow_next_grid();
-    if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], invdt2, fb2);
+    if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tv.tg, invdt2, fb2);
 }
 
 // Dataflow sweeps: a persistent kernel that runs `iterations` colour sweeps with no barrier
@@ -201,22 +197,19 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             }
             break;
         }
-        const int4 h0 = tile_stage(V, S.pos, tile, sb, sd, srec);
+        TileVertex tv;
+        const int4 h0 = tile_stage<G>(V, S, tile, sb, sd, srec, tv);
         const bool active = lv < h0.y;
-        int4 hv = make_int4(0, 0, 0, 0);
-        int roff = 0;
         TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
         if (active) {
-            hv = __ldg(S.hdr + h0.x + lv);
-            roff = __ldg(V.vrec + h0.x + lv);
             cx.bs = v3(sb[lv]);
             cx.ds = v3(sd[lv]);
         }
         Block<float> acc;
         block_zero(acc);
-        tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+        tile_vertex_accumulate<G>(cx, tv.hv, tv.roff, lane, acc);
         group_reduce<G>(acc);
-        if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], invdt2, fb2);
+        if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tv.tg, invdt2, fb2);
         __syncthreads();  // every position of the tile is written (and the staging is consumed)
         if (threadIdx.x == 0) {
             __threadfence();
@@ -249,26 +242,23 @@ __global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileV
     float4 *sb = dyn;
     float4 *sd = dyn + max_local;
     int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
-    const int4 h0 = tile_stage(V, S.pos, blockIdx.x, sb, sd, srec);
+    TileVertex tv;
+    const int4 h0 = tile_stage<G>(V, S, blockIdx.x, sb, sd, srec, tv);
     const int lv = threadIdx.x / G;
     const int lane = threadIdx.x & (G - 1);
     const bool active = lv < h0.y;
-    int4 hv = make_int4(0, 0, 0, 0);
-    int roff = 0;
     TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
     if (active) {
-        hv = __ldg(S.hdr + h0.x + lv);
-        roff = __ldg(V.vrec + h0.x + lv);
         cx.bs = v3(sb[lv]);
         cx.ds = v3(sd[lv]);
     }
     Block<float> acc;
     block_zero(acc);
-    tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+    tile_vertex_accumulate<G>(cx, tv.hv, tv.roff, lane, acc);
     group_reduce<G>(acc);
     double r2 = 0.0;
     if (active && lane == 0) {
-        const float4 tg = S.tgt[h0.x + lv];
+        const float4 tg = tv.tg;
         const double c = double(tg.w) * invdt2;
         const double rx = c * (double(cx.ds.x) - tg.x) - acc.f[0];
         const double ry = c * (double(cx.ds.y) - tg.y) - acc.f[1];

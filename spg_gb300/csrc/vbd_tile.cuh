@@ -62,16 +62,35 @@ struct TileCtx {
     }
 };
 
+// Per-thread data of the tile vertex the thread works on, fetched while the staging copies fly.
+struct TileVertex {
+    int4 hv;     // incidence header
+    int roff;    // record offset inside the tile's block
+    float4 tg;   // inertial target (y - base, mass)
+};
+
 // Stages the tile into shared memory. The tile's records and halo indices never change, so
-// they are fetched before waiting for the previous colour; the positions after. Returns
-// {vstart, nvt, halo_off, n_halo}; thread group threadIdx.x / G owns that tile vertex.
-__device__ __forceinline__ int4 tile_stage(const TileView &V, const float4 *__restrict__ pos, int tile,
-                                           float4 *sb, float4 *sd, int4 *srec)
+// they are fetched before waiting for the previous colour; the positions after. The header
+// and record offset of the thread's vertex (G threads per vertex) are loaded before the wait
+// and its inertial target after it, all while the copies are in flight. Returns
+// {vstart, nvt, halo_off, n_halo}.
+template <int G>
+__device__ __forceinline__ int4 tile_stage(const TileView &V, const DevState &S, int tile, float4 *sb, float4 *sd,
+                                           int4 *srec, TileVertex &tv)
 {
+    const float4 *__restrict__ pos = S.pos;
     const int4 h0 = __ldg(V.hdr + 2 * tile);
     const int4 h1 = __ldg(V.hdr + 2 * tile + 1);
     for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
     const int nvt = h0.y, nl = h0.y + h0.w;
+    const int lv = threadIdx.x / G;
+    tv.hv = make_int4(0, 0, 0, 0);
+    tv.roff = 0;
+    tv.tg = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lv < nvt) {
+        tv.hv = __ldg(S.hdr + h0.x + lv);
+        tv.roff = __ldg(V.vrec + h0.x + lv);
+    }
     constexpr int kMaxHaloPerThread = 8;
     int gidx[kMaxHaloPerThread];
 #pragma unroll
@@ -93,6 +112,7 @@ __device__ __forceinline__ int4 tile_stage(const TileView &V, const float4 *__re
         cp_async16(sb + i, pos + 2 * g);
         cp_async16(sd + i, pos + 2 * g + 1);
     }
+    if (lv < nvt) tv.tg = S.tgt[h0.x + lv];
     cp_async_wait_all();
     __syncthreads();
     return h0;

@@ -98,7 +98,7 @@ def extrapolation_offset(features: np.ndarray) -> np.ndarray:
 
 
 def generate(episodes=16, steps=60, vertices_per_episode=270_000, sizes=(65, 129), keep=1 / 16, tol=1e-5,
-             max_iterations=5000, max_speed=30.0, seed=7, device=0, log=print):
+             max_iterations=3000, max_speed=30.0, seed=7, device=0, time_budget=None, log=print):
     """Runs the episodes on the GPU solver (each step solved to the tolerance, starting from
     the extrapolated guess) and returns (features [m x 24], network targets [m x 3]): the
     recorded (x* - y) / l minus the extrapolated guess's offset.
@@ -112,6 +112,9 @@ def generate(episodes=16, steps=60, vertices_per_episode=270_000, sizes=(65, 129
     feats, targs = [], []
     t0 = time.time()
     for ep in range(episodes):
+        if time_budget is not None and time.time() - t0 > time_budget:
+            log(f"generation time budget reached after {ep} episodes")
+            break
         n = int(sizes[ep % len(sizes)])
         count = max(1, vertices_per_episode // (n * n))
         patches = [random_patch(n, rng) for _ in range(count)]
@@ -142,9 +145,10 @@ def generate(episodes=16, steps=60, vertices_per_episode=270_000, sizes=(65, 129
                     solver.set_state(int(p), patches[p].x, np.zeros_like(patches[p].x))
                 skip = True
         solver.close()
-        rows = ~bad[np.concatenate(ep_p)]
-        feats.append(np.concatenate(ep_f)[rows])
-        targs.append(np.concatenate(ep_t)[rows])
+        if ep_p:
+            rows = ~bad[np.concatenate(ep_p)]
+            feats.append(np.concatenate(ep_f)[rows])
+            targs.append(np.concatenate(ep_t)[rows])
         log(f"episode {ep}: {count} patches of {n}^2 ({int(bad.sum())} folded, dropped), gravity "
             f"{np.round(g, 2).tolist()}, iterations/step mean {np.mean(its):.0f} max {max(its)}, "
             f"{unconverged} steps unconverged, {time.time() - t0:.0f} s")
@@ -191,13 +195,14 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--keep", type=float, default=1 / 16)
     ap.add_argument("--tol", type=float, default=1e-5)
-    ap.add_argument("--max-iterations", type=int, default=5000)
+    ap.add_argument("--max-iterations", type=int, default=3000)
+    ap.add_argument("--time-budget", type=float, default=600.0, help="seconds of data generation at most")
     ap.add_argument("--device", type=int, default=0)
     args = ap.parse_args(argv)
     os.makedirs(args.out, exist_ok=True)
     t0 = time.time()
     X, Y = generate(episodes=args.episodes, steps=args.steps, keep=args.keep, tol=args.tol,
-                    max_iterations=args.max_iterations, device=args.device)
+                    max_iterations=args.max_iterations, device=args.device, time_budget=args.time_budget)
     t_gen = time.time() - t0
     print(f"{X.shape[0]} rows in {t_gen:.0f} s; target rms {np.sqrt(np.mean(Y ** 2)):.4g}", flush=True)
     # Held-out rows (the last 2 %) measure the fit.
