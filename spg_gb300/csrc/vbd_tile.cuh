@@ -139,19 +139,22 @@ __device__ __forceinline__ void tile_vertex_accumulate(const TileCtx &cx, int4 h
         }
         off += n;
     }
-    // Springs, bending flaps and bending hinges take two incidences per round so their
-    // arithmetic forms two independent dependency chains. A missing second incidence is
-    // replaced by a copy of the first with zero stiffness (its contribution is exactly 0).
+    // Springs, bending flaps and bending hinges take two incidences per round where both exist,
+    // so their arithmetic forms two independent dependency chains, and one incidence in the
+    // last round otherwise (6 incidences over 2 lanes: a pair round, then a single round).
     {  // springs: {other, L0, k}
         const int n = (h.y >> 16) & 0xffff;
         const int rounds = warp_max((n + 2 * G - 1) / (2 * G));
         for (int r = 0; r < rounds; ++r) {
             const int i0 = 2 * r * G + lane, i1 = i0 + G;
-            if (i0 < n) {
+            if (i1 < n) {
                 const int4 q0 = cx.rec[off + i0];
-                const int4 q1 = cx.rec[off + (i1 < n ? i1 : i0)];
+                const int4 q1 = cx.rec[off + i1];
                 spring_block(zero, cx.rel(q0.x), __int_as_float(q0.y), __int_as_float(q0.z), acc);
-                spring_block(zero, cx.rel(q1.x), __int_as_float(q1.y), i1 < n ? __int_as_float(q1.z) : 0.f, acc);
+                spring_block(zero, cx.rel(q1.x), __int_as_float(q1.y), __int_as_float(q1.z), acc);
+            } else if (i0 < n) {
+                const int4 q0 = cx.rec[off + i0];
+                spring_block(zero, cx.rel(q0.x), __int_as_float(q0.y), __int_as_float(q0.z), acc);
             }
         }
         off += n;
@@ -161,13 +164,17 @@ __device__ __forceinline__ void tile_vertex_accumulate(const TileCtx &cx, int4 h
         const int rounds = warp_max((n + 2 * G - 1) / (2 * G));
         for (int r = 0; r < rounds; ++r) {
             const int i0 = 2 * r * G + lane, i1 = i0 + G;
-            if (i0 < n) {
+            if (i1 < n) {
                 const int4 q0 = cx.rec[off + i0];
-                const int4 q1 = cx.rec[off + (i1 < n ? i1 : i0)];
+                const int4 q1 = cx.rec[off + i1];
                 bending_flap_block(cx.rel(q0.x & 0xffff), cx.rel(q0.x >> 16), zero, cx.rel(q0.y), __int_as_float(q0.z),
                                    __int_as_float(q0.w), acc);
                 bending_flap_block(cx.rel(q1.x & 0xffff), cx.rel(q1.x >> 16), zero, cx.rel(q1.y), __int_as_float(q1.z),
-                                   i1 < n ? __int_as_float(q1.w) : 0.f, acc);
+                                   __int_as_float(q1.w), acc);
+            } else if (i0 < n) {
+                const int4 q0 = cx.rec[off + i0];
+                bending_flap_block(cx.rel(q0.x & 0xffff), cx.rel(q0.x >> 16), zero, cx.rel(q0.y), __int_as_float(q0.z),
+                                   __int_as_float(q0.w), acc);
             }
         }
         off += n;
@@ -177,13 +184,17 @@ __device__ __forceinline__ void tile_vertex_accumulate(const TileCtx &cx, int4 h
         const int rounds = warp_max((n + 2 * G - 1) / (2 * G));
         for (int r = 0; r < rounds; ++r) {
             const int i0 = 2 * r * G + lane, i1 = i0 + G;
-            if (i0 < n) {
+            if (i1 < n) {
                 const int4 q0 = cx.rec[off + i0];
-                const int4 q1 = cx.rec[off + (i1 < n ? i1 : i0)];
+                const int4 q1 = cx.rec[off + i1];
                 bending_hinge_block(cx.rel(q0.x), zero, cx.rel(q0.y & 0xffff), cx.rel(q0.y >> 16), __int_as_float(q0.z),
                                     __int_as_float(q0.w), acc);
                 bending_hinge_block(cx.rel(q1.x), zero, cx.rel(q1.y & 0xffff), cx.rel(q1.y >> 16), __int_as_float(q1.z),
-                                    i1 < n ? __int_as_float(q1.w) : 0.f, acc);
+                                    __int_as_float(q1.w), acc);
+            } else if (i0 < n) {
+                const int4 q0 = cx.rec[off + i0];
+                bending_hinge_block(cx.rel(q0.x), zero, cx.rel(q0.y & 0xffff), cx.rel(q0.y >> 16), __int_as_float(q0.z),
+                                    __int_as_float(q0.w), acc);
             }
         }
         off += n;

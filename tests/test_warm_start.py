@@ -1,0 +1,92 @@
+"""Initial guesses of the VBD step: the extrapolated guess and the shipped learned network
+against the reference's inertial guess, by iterations to the same residual tolerance
+(GPU), and the host-side pieces of the training pipeline (CPU)."""
+import numpy as np
+import pytest
+
+N = pytest.importorskip("spg_gb300.native")
+from spg_gb300 import warm_start as W  # noqa: E402
+
+
+# ----------------------------------------------------------------------------- CPU
+
+
+def test_random_rotation_is_proper():
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        R = W.random_rotation(rng)
+        assert np.allclose(R @ R.T, np.eye(3), atol=1e-12)
+        assert np.isclose(np.linalg.det(R), 1.0)
+
+
+def test_random_pins_lie_on_the_grid():
+    rng = np.random.default_rng(1)
+    for n in (2, 5, 65):
+        for _ in range(50):
+            p = W.random_pins(n, rng)
+            assert p.size >= 1 and np.all((p >= 0) & (p < n * n)) and np.unique(p).size == p.size
+
+
+def test_extrapolation_offset_and_output_scale_folding():
+    rng = np.random.default_rng(2)
+    f = rng.normal(size=(10, 24)).astype(np.float32)
+    assert np.allclose(W.extrapolation_offset(f), f[:, 3:6] - f[:, 6:9] - f[:, 15:18])
+    from oracle import mlp_ref as M
+    w = rng.normal(size=M.N_PARAMS).astype(np.float32)
+    x = rng.normal(size=(7, 24))
+    y = M.forward(w, x)
+    y2 = M.forward(W.fold_output_scale(w, 0.25), x)
+    # W4 and b4 scale exactly by a power of two, through the BF16 rounding as well
+    assert np.allclose(y2, 0.25 * y, rtol=1e-12, atol=1e-12)
+
+
+def test_shipped_weights_have_the_network_layout():
+    w = np.load(W.WEIGHTS)
+    from oracle import mlp_ref as M
+    assert w.dtype == np.float32 and w.size == M.N_PARAMS and np.all(np.isfinite(w))
+
+
+# ----------------------------------------------------------------------------- GPU
+
+
+def _iterations(mode, mlp=None, n=129, prefix=2, steps=4):
+    from spg_gb300 import scenes as S
+    obj = S.spring_cloth(n).objects[0]
+    s = N.VbdSolver([obj], dt=1 / 120, iterations=20, gravity=(0, 0, -9.81), tolerance=1e-5,
+                    max_iterations=40000, check_interval=50)
+    s.set_warm_start(mlp, mode=mode)
+    its, picks = 0, [0, 0]
+    for k in range(prefix + steps):
+        st = s.step()
+        assert st.converged
+        if k >= prefix:
+            its += st.iterations
+            picks[0] += st.warm_accepted
+            picks[1] += st.extrapolated_accepted
+    s.close()
+    return its, picks
+
+
+@pytest.mark.gpu
+def test_extrapolated_guess_cuts_iterations_to_tolerance():
+    plain, _ = _iterations(0)
+    extrap, picks = _iterations(2)
+    print(f"iterations to 1e-5 over 4 steps: inertial {plain}, extrapolated {extrap}, picks {picks}")
+    assert picks[1] == 4
+    assert plain >= 1.5 * max(extrap, 1)
+
+
+@pytest.mark.gpu
+def test_learned_guess_with_the_shipped_network():
+    """The learned mode (extrapolation plus the shipped network's correction, started from
+    the lowest-residual guess) reaches the tolerance in at most 2/3 of the inertial guess's
+    iterations, and never needs more than the extrapolated guess alone by more than the
+    check granularity."""
+    mlp = W.load_mlp()
+    plain, _ = _iterations(0)
+    learned, picks = _iterations(1, mlp)
+    extrap, _ = _iterations(2)
+    print(f"iterations to 1e-5 over 4 steps: inertial {plain}, extrapolated {extrap}, learned {learned} "
+          f"(network's guess picked {picks[0]}x, extrapolated {picks[1]}x)")
+    assert plain >= 1.5 * max(learned, 1)
+    assert learned <= extrap + 4 * 50
