@@ -46,7 +46,18 @@ typedef enum spgx_energy_type {
     SPGX_ENERGY_SPRING_ANCHOR = 2,      /* spg::SpringAnchorEnergy       springAnchorEnergy.h:7 */
     SPGX_ENERGY_DISCRETE_BENDING = 3,   /* spg::DiscreteBendingEnergy    discreteBendingEnergy.h:9 */
     SPGX_ENERGY_MEMBRANE_STVK = 4,      /* spg::MembraneStvkEnergy       membraneStvkEnergy.h:9 */
-    SPGX_ENERGY_STABLE_NEO_HOOKEAN = 5  /* spg::StableNeoHookeanEnergy   stableNeoHookeanEnergy.h:10 */
+    SPGX_ENERGY_STABLE_NEO_HOOKEAN = 5, /* spg::StableNeoHookeanEnergy   stableNeoHookeanEnergy.h:10 */
+    /* The types below run on the lanes-per-vertex kernel (kernel 1) with per-vertex forward-mode
+     * derivatives on the device, and are not accepted by the XPBD solver. */
+    SPGX_ENERGY_STVK = 6,                         /* spg::StvkEnergy (tet)              stvkEnergy.h */
+    SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN = 7,   /* spg::StableSquaredNeoHookeanEnergy */
+    SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN = 8,       /* spg::MembraneBaraffWitkinEnergy */
+    SPGX_ENERGY_MEMBRANE_CHOI = 9,                /* spg::MembraneChoiEnergy */
+    SPGX_ENERGY_BARAFF_WITKIN_BENDING = 10,       /* spg::BaraffWitkinBendingEnergy */
+    SPGX_ENERGY_QUADRATIC_BENDING = 11,           /* spg::QuadraticBendingEnergy */
+    SPGX_ENERGY_SPRING_CONTINUUM = 12,            /* spg::SpringContinuumEnergy */
+    SPGX_ENERGY_SPRING_SQUARED_CONTINUUM = 13,    /* spg::SpringSquaredContinuumEnergy */
+    SPGX_ENERGY_STATIC_LOAD = 14                  /* spg::StaticLoadEnergy */
 } spgx_energy_type;
 
 /*
@@ -61,7 +72,20 @@ typedef enum spgx_energy_type {
  *   STABLE_NEO_HOOKEAN [inverseReferenceMat (3x3 row-major), effectiveStiffness(0,0),
  *                      effectiveStiffness(1,1), hydrostaticCorrectionTerm,
  *                      effectiveCompliance(0,0), effectiveCompliance(1,1)]
- * i.e. the values the reference holds after addStencil() and preparePrecomputations().
+ *   STVK, STABLE_SQUARED_NEO_HOOKEAN
+ *                     [inverseReferenceMat (3x3 row-major), effectiveStiffness(0,0) (lambda V),
+ *                      effectiveStiffness(1,1) (mu V), effectiveCompliance(0,0), (1,1)]
+ *   MEMBRANE_BARAFF_WITKIN [inverseReferenceMat (2x2 row-major), effectiveStiffness diagonal (3),
+ *                      effectiveCompliance diagonal (3)]
+ *   MEMBRANE_CHOI     [inverseReferenceMat (2x2 row-major), effectiveStiffness diagonal (4),
+ *                      effectiveCompliance diagonal (4)]
+ *   BARAFF_WITKIN_BENDING [restTheta, effectiveStiffness, effectiveCompliance]
+ *   QUADRATIC_BENDING [laplacian weights c0..c3 (laplacians()[i](0, 0), (0, 3), (0, 6), (0, 9)),
+ *                      effectiveStiffness(0,0), effectiveCompliance(0,0)]
+ *   SPRING_CONTINUUM, SPRING_SQUARED_CONTINUUM [restLength, effectiveStiffness, effectiveCompliance]
+ *   STATIC_LOAD       [modelStiffness, loadDirection.x, .y, .z]
+ * i.e. the values the reference holds after addStencil() and preparePrecomputations(). The
+ * stiffness matrices of types 6-13 are diagonal, so only their diagonals are passed.
  */
 typedef struct spgx_energy_desc {
     int32_t type;

@@ -168,6 +168,13 @@ inline Dual<N, Hs> atan2(const Dual<N, Hs> &y, const Dual<N, Hs> &x)
 
 // Plain-double overloads so templated energy code can be instantiated on double.
 inline double sqrt(double a) { return std::sqrt(a); }
+// The value of a scalar with its derivatives dropped (TinyAD's `.val`).
+inline double value_of(double a) { return a; }
+template <int N, bool Hs>
+inline double value_of(const Dual<N, Hs> &a)
+{
+    return a.val;
+}
 inline double atan2(double y, double x) { return std::atan2(y, x); }
 
 template <typename T>

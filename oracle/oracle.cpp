@@ -694,6 +694,23 @@ static void incidence_block(int type, const double *X, const int *st, const doub
         ad_block<4>([](const auto *q, const double *pp) { return snh_energy(q, pp); }, p, params, slot, mode, g, H);
         break;
     }
+#define ORACLE_GENERIC_CASE(KIND, S, FN)                                                                          \
+    case KIND: {                                                                                                  \
+        V3<double> p[S];                                                                                          \
+        load_stencil<S>(X, st, p);                                                                                \
+        ad_block<S>([](const auto *q, const double *pp) { return FN(q, pp); }, p, params, slot, mode, g, H);       \
+        break;                                                                                                    \
+    }
+        ORACLE_GENERIC_CASE(kStvkTet, 4, stvk_tet_energy)
+        ORACLE_GENERIC_CASE(kSsnh, 4, ssnh_energy)
+        ORACLE_GENERIC_CASE(kBwMembrane, 3, bw_membrane_energy)
+        ORACLE_GENERIC_CASE(kChoi, 3, choi_energy)
+        ORACLE_GENERIC_CASE(kBwBending, 4, bw_bending_energy)
+        ORACLE_GENERIC_CASE(kQuadBending, 4, quad_bending_energy)
+        ORACLE_GENERIC_CASE(kSpringCont, 2, spring_cont_energy)
+        ORACLE_GENERIC_CASE(kSpringSqCont, 2, spring_sq_cont_energy)
+        ORACLE_GENERIC_CASE(kStaticLoad, 1, static_load_energy)
+#undef ORACLE_GENERIC_CASE
     default: throw std::runtime_error("unsupported energy type");
     }
 }
@@ -706,6 +723,15 @@ static double element_energy(int type, const V3<double> *p, const double *params
     case kBending: return bending_energy(p, params);
     case kStvk: return stvk_energy(p, params);
     case kSnh: return snh_energy(p, params);
+    case kStvkTet: return stvk_tet_energy(p, params);
+    case kSsnh: return ssnh_energy(p, params);
+    case kBwMembrane: return bw_membrane_energy(p, params);
+    case kChoi: return choi_energy(p, params);
+    case kBwBending: return bw_bending_energy(p, params);
+    case kQuadBending: return quad_bending_energy(p, params);
+    case kSpringCont: return spring_cont_energy(p, params);
+    case kSpringSqCont: return spring_sq_cont_energy(p, params);
+    case kStaticLoad: return static_load_energy(p, params);
     default: throw std::runtime_error("unsupported energy type");
     }
 }
@@ -732,6 +758,12 @@ static int n_constraints(int type)
     switch (type) {
     case kStvk: return 3;
     case kSnh: return 2;
+    case kStvkTet: return 2;
+    case kSsnh: return 2;
+    case kBwMembrane: return 3;
+    case kChoi: return 4;
+    case kQuadBending: return 3;
+    case kStaticLoad: return 0;
     default: return 1;
     }
 }
@@ -758,6 +790,39 @@ static void element_constraints(int type, const V3<double> *p, const double *par
     case kSnh:
         constraints_and_gradient<4, 2>([](const auto *q, const double *pp, auto *c) { snh_constraints(q, pp, c); }, p,
                                        params, C, gradC);
+        break;
+    case kStvkTet:
+        constraints_and_gradient<4, 2>([](const auto *q, const double *pp, auto *c) { stvk_tet_constraints(q, pp, c); },
+                                       p, params, C, gradC);
+        break;
+    case kSsnh:
+        constraints_and_gradient<4, 2>([](const auto *q, const double *pp, auto *c) { ssnh_constraints(q, pp, c); }, p,
+                                       params, C, gradC);
+        break;
+    case kBwMembrane:
+        constraints_and_gradient<3, 3>([](const auto *q, const double *pp, auto *c) { bw_membrane_constraints(q, pp, c); },
+                                       p, params, C, gradC);
+        break;
+    case kChoi:
+        constraints_and_gradient<3, 4>([](const auto *q, const double *pp, auto *c) { choi_constraints(q, pp, c); }, p,
+                                       params, C, gradC);
+        break;
+    case kBwBending:
+        constraints_and_gradient<4, 1>(
+            [](const auto *q, const double *pp, auto *c) { c[0] = bw_bending_constraint(q, pp); }, p, params, C, gradC);
+        break;
+    case kQuadBending:
+        constraints_and_gradient<4, 3>([](const auto *q, const double *pp, auto *c) { quad_bending_constraints(q, pp, c); },
+                                       p, params, C, gradC);
+        break;
+    case kSpringCont:
+        constraints_and_gradient<2, 1>(
+            [](const auto *q, const double *pp, auto *c) { c[0] = spring_cont_constraint(q, pp); }, p, params, C, gradC);
+        break;
+    case kSpringSqCont:
+        constraints_and_gradient<2, 1>(
+            [](const auto *q, const double *pp, auto *c) { c[0] = spring_sq_cont_constraint(q, pp); }, p, params, C,
+            gradC);
         break;
     default: throw std::runtime_error("unsupported energy type");
     }
@@ -1396,6 +1461,15 @@ int oracle_element_full(int type, const double *X, const double *params, double 
     case kBending: fill([](const auto *q, const double *pp) { return bending_energy(q, pp); }, std::integral_constant<int, 4>{}); break;
     case kStvk: fill([](const auto *q, const double *pp) { return stvk_energy(q, pp); }, std::integral_constant<int, 3>{}); break;
     case kSnh: fill([](const auto *q, const double *pp) { return snh_energy(q, pp); }, std::integral_constant<int, 4>{}); break;
+    case kStvkTet: fill([](const auto *q, const double *pp) { return stvk_tet_energy(q, pp); }, std::integral_constant<int, 4>{}); break;
+    case kSsnh: fill([](const auto *q, const double *pp) { return ssnh_energy(q, pp); }, std::integral_constant<int, 4>{}); break;
+    case kBwMembrane: fill([](const auto *q, const double *pp) { return bw_membrane_energy(q, pp); }, std::integral_constant<int, 3>{}); break;
+    case kChoi: fill([](const auto *q, const double *pp) { return choi_energy(q, pp); }, std::integral_constant<int, 3>{}); break;
+    case kBwBending: fill([](const auto *q, const double *pp) { return bw_bending_energy(q, pp); }, std::integral_constant<int, 4>{}); break;
+    case kQuadBending: fill([](const auto *q, const double *pp) { return quad_bending_energy(q, pp); }, std::integral_constant<int, 4>{}); break;
+    case kSpringCont: fill([](const auto *q, const double *pp) { return spring_cont_energy(q, pp); }, std::integral_constant<int, 2>{}); break;
+    case kSpringSqCont: fill([](const auto *q, const double *pp) { return spring_sq_cont_energy(q, pp); }, std::integral_constant<int, 2>{}); break;
+    case kStaticLoad: fill([](const auto *q, const double *pp) { return static_load_energy(q, pp); }, std::integral_constant<int, 1>{}); break;
     default: return 1;
     }
     return 0;

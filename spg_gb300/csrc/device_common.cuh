@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include "elements.cuh"
+#include "generic.cuh"
 
 namespace spgx {
 
@@ -37,6 +38,15 @@ struct DevTables {
     const float4 *snh_p2;
     const float2 *snh_cmp;
     const float2 *anchor_cmp;
+    // Energies of types 6-14: per internal vertex gen_off[v]..gen_off[v+1] in gen_adj
+    // ((element << 2) | slot); per element its vertices (gen_idx, -1 padded) and
+    // {type, parameter offset, stencil size, 0} (gen_info); parameters in gen_prm.
+    // gen_off is null when the scene has none.
+    const int *gen_off;
+    const int *gen_adj;
+    const int4 *gen_idx;
+    const int4 *gen_info;
+    const float *gen_prm;
 };
 
 constexpr int kCounters = 8;
@@ -94,12 +104,13 @@ __device__ __forceinline__ int ld_relaxed_gpu(const int *p)
 
 
 // Walks the vertex's class-sorted incidence list with G lanes per vertex (lane-strided) and
-// accumulates the force and Hessian block of every incident element into acc.
+// accumulates the force and Hessian block of every incident element into acc; with kGeneric
+// also the vertex's incidences of energy types 6-14 (T.gen_off must then be set).
 // Loop trip counts are warp-uniform (max over the warp), so all 32 lanes stay converged.
-template <int G>
+template <int G, bool kGeneric = false>
 __device__ __forceinline__ void accumulate_incidences(const DevTables &T, const float4 *__restrict__ pos,
                                                       const int *__restrict__ adj, int4 h, int lane, V3f bs, V3f ds,
-                                                      Block<float> &acc)
+                                                      Block<float> &acc, int v)
 {
     int off = h.x;
     const V3f zero = mk(0.f, 0.f, 0.f);
@@ -220,6 +231,32 @@ __device__ __forceinline__ void accumulate_incidences(const DevTables &T, const 
                 p[3] = slot == 3 ? zero : rel_pos(pos, st.w, bs, ds);
                 const float D[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
                 snh_block(p, slot, D, c.y, c.z, c.w, acc);
+            }
+        }
+    }
+    // Energies of types 6-14 (v < 0: inactive lane of a partial group). A separate kernel
+    // instantiation, so scenes without them keep the lean register budget.
+    if (kGeneric) {
+        int b = 0, n = 0;
+        if (v >= 0) {
+            b = __ldg(T.gen_off + v);
+            n = __ldg(T.gen_off + v + 1) - b;
+        }
+        const int rounds = warp_max((n + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < n) {
+                const int ent = __ldg(T.gen_adj + b + i);
+                const int e = ent >> 2;
+                const int slot = ent & 3;
+                const int4 ix = __ldg(T.gen_idx + e);
+                const int4 info = __ldg(T.gen_info + e);
+                const int iv[4] = {ix.x, ix.y, ix.z, ix.w};
+                V3f p[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    p[j] = (j >= info.z || j == slot) ? zero : rel_pos(pos, iv[j], bs, ds);
+                generic_block(info.x, p, slot, T.gen_prm + info.y, acc);
             }
         }
     }

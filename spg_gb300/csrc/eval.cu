@@ -45,10 +45,16 @@ __global__ void eval_blocks_kernel(int type, int n, int S, int P, const float *_
         stvk_block(r, slot, D, Ks, b);
         break;
     }
-    default: {
+    case SPGX_ENERGY_STABLE_NEO_HOOKEAN: {
         float D[9];
         for (int k = 0; k < 9; ++k) D[k] = p[k];
         snh_block(r, slot, D, p[9], p[10], p[11], b);
+        break;
+    }
+    default: {
+        V3f q[4];
+        for (int j = 0; j < 4; ++j) q[j] = j < S ? r[j] : zero;
+        generic_block(type, q, slot, p, b);
         break;
     }
     }

@@ -16,6 +16,15 @@ int stencil_size(int type)
     case SPGX_ENERGY_DISCRETE_BENDING: return 4;
     case SPGX_ENERGY_MEMBRANE_STVK: return 3;
     case SPGX_ENERGY_STABLE_NEO_HOOKEAN: return 4;
+    case SPGX_ENERGY_STVK: return 4;
+    case SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN: return 4;
+    case SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN: return 3;
+    case SPGX_ENERGY_MEMBRANE_CHOI: return 3;
+    case SPGX_ENERGY_BARAFF_WITKIN_BENDING: return 4;
+    case SPGX_ENERGY_QUADRATIC_BENDING: return 4;
+    case SPGX_ENERGY_SPRING_CONTINUUM: return 2;
+    case SPGX_ENERGY_SPRING_SQUARED_CONTINUUM: return 2;
+    case SPGX_ENERGY_STATIC_LOAD: return 1;
     default: return 0;
     }
 }
@@ -28,6 +37,15 @@ int param_count(int type)
     case SPGX_ENERGY_DISCRETE_BENDING: return 3;
     case SPGX_ENERGY_MEMBRANE_STVK: return 22;
     case SPGX_ENERGY_STABLE_NEO_HOOKEAN: return 14;
+    case SPGX_ENERGY_STVK: return 13;
+    case SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN: return 13;
+    case SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN: return 10;
+    case SPGX_ENERGY_MEMBRANE_CHOI: return 12;
+    case SPGX_ENERGY_BARAFF_WITKIN_BENDING: return 3;
+    case SPGX_ENERGY_QUADRATIC_BENDING: return 6;
+    case SPGX_ENERGY_SPRING_CONTINUUM: return 3;
+    case SPGX_ENERGY_SPRING_SQUARED_CONTINUUM: return 3;
+    case SPGX_ENERGY_STATIC_LOAD: return 4;
     default: return 0;
     }
 }
@@ -286,6 +304,7 @@ spgx_status build_scene_layout(const spgx_scene_desc *scene, bool with_xpbd, Sce
     auto &T = L.el;
     L.elem_base.resize(nobj);
     std::vector<int64_t> cls_count(size_t(nv) * kNumClasses, 0);
+    std::vector<int64_t> gen_count(size_t(nv), 0);
     for (int o = 0; o < nobj; ++o) {
         const auto &ob = scene->objects[o];
         const int vb = L.objects[o].vertex_base;
@@ -299,6 +318,14 @@ spgx_status build_scene_layout(const spgx_scene_desc *scene, bool with_xpbd, Sce
                 const double *p = E.params + int64_t(s) * P;
                 int iv[4] = {0, 0, 0, 0};
                 for (int k = 0; k < S; ++k) iv[k] = L.ext2int[vb + st[k]];
+                if (is_generic_type(E.type)) {
+                    if (s == 0) eb = static_cast<int32_t>(T.gen_idx.size());
+                    T.gen_idx.push_back({iv[0], S > 1 ? iv[1] : -1, S > 2 ? iv[2] : -1, S > 3 ? iv[3] : -1});
+                    T.gen_info.push_back({E.type, static_cast<int32_t>(T.gen_prm.size()), S, 0});
+                    for (int k = 0; k < P; ++k) T.gen_prm.push_back(static_cast<float>(p[k]));
+                    for (int k = 0; k < S; ++k) ++gen_count[iv[k]];
+                    continue;
+                }
                 switch (E.type) {
                 case SPGX_ENERGY_SPRING_ANCHOR:
                     if (s == 0) eb = static_cast<int32_t>(T.anchors.size());
@@ -343,7 +370,8 @@ spgx_status build_scene_layout(const spgx_scene_desc *scene, bool with_xpbd, Sce
             L.elem_base[o].push_back(eb);
         }
     }
-    const size_t n_elems = T.anchors.size() + T.springs.size() + T.bend_idx.size() + T.stvk_idx.size() + T.snh_idx.size();
+    const size_t n_elems = T.anchors.size() + T.springs.size() + T.bend_idx.size() + T.stvk_idx.size() +
+                           T.snh_idx.size() + T.gen_idx.size();
     if (n_elems >= (size_t(1) << 29)) {
         err = "too many elements";
         return SPGX_ERR_INVALID_ARG;
@@ -361,13 +389,26 @@ spgx_status build_scene_layout(const spgx_scene_desc *scene, bool with_xpbd, Sce
             tot += n;
         }
         voff[v + 1] = voff[v] + tot;
-        L.max_degree = std::max<int>(L.max_degree, static_cast<int>(tot));
+        L.max_degree = std::max<int>(L.max_degree, static_cast<int>(tot + gen_count[v]));
     }
     if (voff[nv] >= (int64_t(1) << 31)) {
         err = "too many incidences";
         return SPGX_ERR_INVALID_ARG;
     }
-    L.mean_degree = nv ? double(voff[nv]) / nv : 0.0;
+    int64_t n_gen = 0;
+    for (int v = 0; v < nv; ++v) n_gen += gen_count[v];
+    if (n_gen >= (int64_t(1) << 31)) {
+        err = "too many incidences";
+        return SPGX_ERR_INVALID_ARG;
+    }
+    L.mean_degree = nv ? double(voff[nv] + n_gen) / nv : 0.0;
+    std::vector<int64_t> gen_fill;
+    if (n_gen > 0) {
+        L.gen_off.assign(size_t(nv) + 1, 0);
+        for (int v = 0; v < nv; ++v) L.gen_off[v + 1] = L.gen_off[v] + static_cast<int32_t>(gen_count[v]);
+        L.gen_adj.assign(size_t(n_gen), 0);
+        gen_fill.assign(L.gen_off.begin(), L.gen_off.end() - 1);
+    }
     L.hdr.resize(nv);
     std::vector<int64_t> cls_fill(size_t(nv) * kNumClasses);
     for (int v = 0; v < nv; ++v) {
@@ -392,6 +433,10 @@ spgx_status build_scene_layout(const spgx_scene_desc *scene, bool with_xpbd, Sce
             for (int64_t i = 0; i < int64_t(E.n_stencils) * S; ++i) {
                 const int slot = static_cast<int>(i % S);
                 const int iv = L.ext2int[vb + E.stencils[i]];
+                if (is_generic_type(E.type)) {
+                    L.gen_adj[gen_fill[iv]++] = static_cast<int32_t>(((eb + i / S) << 2) | slot);
+                    continue;
+                }
                 const int64_t k = cls_fill[size_t(iv) * kNumClasses + incidence_class(E.type, slot)]++;
                 L.adj[k] = static_cast<int32_t>(((eb + i / S) << 2) | slot);
             }

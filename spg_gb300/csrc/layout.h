@@ -62,6 +62,11 @@ struct ElementTables {
     std::vector<F4> snh_p1;        // D11 D12 D20 D21
     std::vector<F4> snh_p2;        // D22 lambda mu alpha
     std::vector<F2> snh_cmp;       // compliance (0,0), (1,1)
+    // Types 6-14 (generic per-vertex derivatives): vertices (-1 padded), {type, param offset,
+    // stencil size, 0}, parameters (the spgx.h layout, FP32).
+    std::vector<I4> gen_idx;
+    std::vector<I4> gen_info;
+    std::vector<float> gen_prm;
 };
 
 struct SceneLayout {
@@ -75,12 +80,15 @@ struct SceneLayout {
     std::vector<double> v_ext;         // 3 * nv external order
     std::vector<I4> hdr;               // per internal vertex: offset, counts (16-bit pairs)
     std::vector<int32_t> adj;          // (element << 2) | slot, class-sorted per vertex
+    std::vector<int32_t> gen_off;      // types 6-14: per internal vertex, range in gen_adj (empty if none)
+    std::vector<int32_t> gen_adj;      // (generic element << 2) | slot, reference order per vertex
     ElementTables el;
     // Per-type element offset of each (object, energy) in the device tables.
     std::vector<std::vector<int32_t>> elem_base;
     std::vector<ObjectLayout> objects;
     int max_degree{0};
     double mean_degree{0};
+    bool gen_idx_empty() const { return el.gen_idx.empty(); }
 };
 
 // Tiles of one colour for the shared-memory VBD kernel. A tile is a run of consecutive
@@ -108,6 +116,8 @@ struct TileLayout {
 spgx_status build_tiles(const SceneLayout &L, int tile_vertices, TileLayout &out, std::string &err);
 
 int stencil_size(int type);
+// Types 6-14 run through the generic per-vertex derivative path (lanes kernel only).
+inline bool is_generic_type(int type) { return type >= SPGX_ENERGY_STVK && type <= SPGX_ENERGY_STATIC_LOAD; }
 int param_count(int type);
 
 // Greedy first-fit vertex colouring in index order (graphColoring.cpp:21-49, 72-84),

@@ -86,7 +86,7 @@ __device__ __forceinline__ void solve_and_update(const DevState &S, int v, const
 }
 
 // One colour phase: G lanes per vertex over the vertices [cstart, cend) of one colour.
-template <int G>
+template <int G, bool kGeneric>
 __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const DevState S, int cstart, int cend,
                                                         float invdt2, float fb2)
 {
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
     }
     Block<float> acc;
     block_zero(acc);
-    accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
+    accumulate_incidences<G, kGeneric>(T, S.pos, S.adj, h, lane, bs, ds, acc, active ? v : -1);
     group_reduce<G>(acc);
     allow_next_grid();
     if (active && lane == 0) solve_and_update(S, v, acc, S.pos[2 * v + 1], S.tgt[v], invdt2, fb2);
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileV
 }
 
 // ||M/h^2 (x - y) + grad E(x)||^2 with per-vertex FP32 forces and an FP64 reduction.
-template <int G>
+template <int G, bool kGeneric>
 __global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const DevState S, int nv, float invdt2,
                                                        double *out)
 {
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const 
     }
     Block<float> acc;
     block_zero(acc);
-    accumulate_incidences<G>(T, S.pos, S.adj, h, lane, bs, ds, acc);
+    accumulate_incidences<G, kGeneric>(T, S.pos, S.adj, h, lane, bs, ds, acc, active ? v : -1);
     group_reduce<G>(acc);
     double r2 = 0.0;
     if (active && lane == 0) {
@@ -324,6 +324,34 @@ static void launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t sme
     cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
+template <bool kGeneric>
+static void launch_lanes(int lanes, int grid, int block, cudaStream_t st, const DevTables &T, const DevState &S,
+                         int cs, int ce, float invdt2, float fb2)
+{
+    switch (lanes) {
+    case 1: vbd_color_kernel<1, kGeneric><<<grid, block, 0, st>>>(T, S, cs, ce, invdt2, fb2); break;
+    case 2: vbd_color_kernel<2, kGeneric><<<grid, block, 0, st>>>(T, S, cs, ce, invdt2, fb2); break;
+    case 4: vbd_color_kernel<4, kGeneric><<<grid, block, 0, st>>>(T, S, cs, ce, invdt2, fb2); break;
+    case 8: vbd_color_kernel<8, kGeneric><<<grid, block, 0, st>>>(T, S, cs, ce, invdt2, fb2); break;
+    case 16: vbd_color_kernel<16, kGeneric><<<grid, block, 0, st>>>(T, S, cs, ce, invdt2, fb2); break;
+    default: vbd_color_kernel<32, kGeneric><<<grid, block, 0, st>>>(T, S, cs, ce, invdt2, fb2); break;
+    }
+}
+
+template <bool kGeneric>
+static void launch_residual_lanes(int lanes, int grid, int block, cudaStream_t st, const DevTables &T,
+                                  const DevState &S, int nv, float invdt2, double *out)
+{
+    switch (lanes) {
+    case 1: residual_kernel<1, kGeneric><<<grid, block, 0, st>>>(T, S, nv, invdt2, out); break;
+    case 2: residual_kernel<2, kGeneric><<<grid, block, 0, st>>>(T, S, nv, invdt2, out); break;
+    case 4: residual_kernel<4, kGeneric><<<grid, block, 0, st>>>(T, S, nv, invdt2, out); break;
+    case 8: residual_kernel<8, kGeneric><<<grid, block, 0, st>>>(T, S, nv, invdt2, out); break;
+    case 16: residual_kernel<16, kGeneric><<<grid, block, 0, st>>>(T, S, nv, invdt2, out); break;
+    default: residual_kernel<32, kGeneric><<<grid, block, 0, st>>>(T, S, nv, invdt2, out); break;
+    }
+}
+
 static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
 {
     if (s.kernel == 2) {
@@ -347,14 +375,11 @@ static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
     const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
     // Launched without programmatic overlap: this kernel reads neighbour positions through the
     // read-only data path, which must not run while the previous colour still writes them.
-    switch (s.lanes) {
-    case 1: vbd_color_kernel<1><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
-    case 2: vbd_color_kernel<2><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
-    case 4: vbd_color_kernel<4><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
-    case 8: vbd_color_kernel<8><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
-    case 16: vbd_color_kernel<16><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
-    default: vbd_color_kernel<32><<<grid, s.block, 0, st>>>(s.T, s.S, cs, ce, invdt2, fb2); break;
+    if (s.T.gen_off) {
+        launch_lanes<true>(s.lanes, grid, s.block, st, s.T, s.S, cs, ce, invdt2, fb2);
+        return;
     }
+    launch_lanes<false>(s.lanes, grid, s.block, st, s.T, s.S, cs, ce, invdt2, fb2);
 }
 
 // n sweeps of the dataflow kernel in one cooperative launch (one resident wave of CTAs).
@@ -434,18 +459,30 @@ static void launch_residual(const VbdSolver &s, cudaStream_t st, double *out = n
         return;
     }
     const int grid = ceil_div(static_cast<long long>(s.L.nv) * s.lanes, s.block);
-    switch (s.lanes) {
-    case 1: residual_kernel<1><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
-    case 2: residual_kernel<2><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
-    case 4: residual_kernel<4><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
-    case 8: residual_kernel<8><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
-    case 16: residual_kernel<16><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
-    default: residual_kernel<32><<<grid, s.block, 0, st>>>(s.T, s.S, s.L.nv, invdt2, out); break;
-    }
+    if (s.T.gen_off)
+        launch_residual_lanes<true>(s.lanes, grid, s.block, st, s.T, s.S, s.L.nv, invdt2, out);
+    else
+        launch_residual_lanes<false>(s.lanes, grid, s.block, st, s.T, s.S, s.L.nv, invdt2, out);
 }
 
 // ---------------------------------------------------------------------------------------
 // Solver methods
+
+spgx_status ElementBuffers::upload_generic(const SceneLayout &L, DevTables &T)
+{
+    if (L.gen_off.empty()) return SPGX_OK;
+    SPGX_TRY_STATUS(gen_off.upload(L.gen_off));
+    SPGX_TRY_STATUS(gen_adj.upload(L.gen_adj));
+    SPGX_TRY_STATUS(gen_idx.upload(L.el.gen_idx));
+    SPGX_TRY_STATUS(gen_info.upload(L.el.gen_info));
+    SPGX_TRY_STATUS(gen_prm.upload(L.el.gen_prm));
+    T.gen_off = gen_off.as<int>();
+    T.gen_adj = gen_adj.as<int>();
+    T.gen_idx = gen_idx.as<int4>();
+    T.gen_info = gen_info.as<int4>();
+    T.gen_prm = gen_prm.as<float>();
+    return SPGX_OK;
+}
 
 spgx_status ElementBuffers::upload(const ElementTables &E, DevTables &T)
 {
@@ -507,6 +544,7 @@ spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params 
     SPGX_CUDA(cudaEventCreate(&ev1));
     SPGX_TRY_STATUS(X.init(L));
     SPGX_TRY_STATUS(EB.upload(L.el, T));
+    SPGX_TRY_STATUS(EB.upload_generic(L, T));
     SPGX_TRY_STATUS(d_hdr.upload(L.hdr));
     SPGX_TRY_STATUS(d_adj.upload(L.adj));
     SPGX_TRY_STATUS(d_counters.alloc(kCounters * sizeof(int)));
@@ -700,8 +738,15 @@ spgx_status VbdSolver::configure_launch()
     };
     std::vector<Cand> cands;
     const bool want_lanes = P.kernel == 0 || P.kernel == 1;
-    const bool want_tiles = P.kernel == 0 || P.kernel == 2;
-    const bool want_flow = P.kernel == 0 || P.kernel == 3;
+    // Energies of types 6-14 are evaluated by the lanes kernel only (they are not in the
+    // tile records).
+    const bool generic = !L.gen_off.empty();
+    if (generic && (P.kernel == 2 || P.kernel == 3)) {
+        set_error("energy types 6-14 run on the lanes-per-vertex kernel (kernel 1) only");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    const bool want_tiles = !generic && (P.kernel == 0 || P.kernel == 2);
+    const bool want_flow = !generic && (P.kernel == 0 || P.kernel == 3);
     std::vector<int> blocks;
     if (P.block_size)
         blocks.push_back(P.block_size);

@@ -16,7 +16,10 @@ namespace spgx {
 struct ElementBuffers {
     DevBuf anchors, springs, spring_cmp, bend_idx, bend_prm, stvk_idx, stvk_D, stvk_Ka, stvk_Kb, stvk_Ca, stvk_Cb,
         stvk_Cc, snh_idx, snh_p0, snh_p1, snh_p2, snh_cmp, anchor_cmp;
+    DevBuf gen_off, gen_adj, gen_idx, gen_info, gen_prm;
     spgx_status upload(const ElementTables &E, DevTables &T);
+    // Energies of types 6-14 (no-op without them).
+    spgx_status upload_generic(const SceneLayout &L, DevTables &T);
 };
 
 struct VbdSolver {

@@ -35,6 +35,13 @@ void build_vertex_neighbours(const SceneLayout &L, std::vector<int32_t> &off, st
         for (int a = 0; a < 4; ++a)
             for (int b = a + 1; b < 4; ++b) link(v[a], v[b]);
     }
+    for (size_t e = 0; e < E.gen_idx.size(); ++e) {  // types 6-14: every pair of the stencil
+        const I4 t = E.gen_idx[e];
+        const int v[4] = {t.x, t.y, t.z, t.w};
+        const int S = E.gen_info[e].z;
+        for (int a = 0; a < S; ++a)
+            for (int b = a + 1; b < S; ++b) link(v[a], v[b]);
+    }
     std::vector<char> anchored(nv, 0);
     for (int32_t v : E.anchor_v) anchored[v] = 1;
     off.assign(nv + 1, 0);

@@ -243,6 +243,10 @@ struct XpbdSolver {
             set_error(err);
             return st;
         }
+        if (!L.gen_idx_empty()) {
+            set_error("the XPBD solver supports energy types 1-5 only");
+            return SPGX_ERR_UNSUPPORTED_ENERGY;
+        }
         SPGX_TRY_STATUS(check_params(params));
         P = *params;
         h_sub = P.dt / P.substeps;

@@ -1,94 +1,9 @@
-// Packing of ParticleGroups into the C ABI descriptor and the GpuVBD / GpuXPBD drop-in solvers.
+// The GpuVBD / GpuXPBD drop-in solvers (packing: pack.cpp).
 #include <stdexcept>
 #include <typeinfo>
 
 #include "spg/sim/solver/gpuPacking.h"
 #include "spg/sim/solver/gpuSolvers.h"
-
-namespace spg::gpu {
-
-void pack(const ParticleGroup &g, PackedObject &out)
-{
-    const int nv = g.size();
-    out = PackedObject();
-    out.x.resize(3 * nv);
-    out.v.resize(3 * nv);
-    out.mass.assign(g.masses().begin(), g.masses().end());
-    for (int i = 0; i < nv; ++i)
-        for (int a = 0; a < 3; ++a) {
-            out.x[3 * i + a] = g.positions()[i][a];
-            out.v[3 * i + a] = g.velocities()[i][a];
-        }
-    for (const auto &ep : g.energies()) {
-        const auto *e = ep.get();
-        std::vector<int32_t> st;
-        for (int s : e->flatStencils()) st.push_back(s);
-        std::vector<double> p;
-        int type = 0;
-        if (auto *sp = dynamic_cast<const SpringEnergy *>(e)) {
-            type = SPGX_ENERGY_SPRING;
-            for (int i = 0; i < sp->nStencils(); ++i)
-                p.insert(p.end(), {sp->restLengths()[i], sp->effectiveStiffness()[i](0, 0),
-                                   sp->effectiveCompliance()[i](0, 0)});
-        } else if (auto *an = dynamic_cast<const SpringAnchorEnergy *>(e)) {
-            type = SPGX_ENERGY_SPRING_ANCHOR;
-            for (int i = 0; i < an->nStencils(); ++i)
-                p.insert(p.end(), {an->anchors()[i][0], an->anchors()[i][1], an->anchors()[i][2],
-                                   an->modelStiffness()[i](0, 0), an->effectiveCompliance()[i](0, 0)});
-        } else if (auto *bd = dynamic_cast<const DiscreteBendingEnergy *>(e)) {
-            type = SPGX_ENERGY_DISCRETE_BENDING;
-            for (int i = 0; i < bd->nStencils(); ++i)
-                p.insert(p.end(), {bd->restThetas()[i], bd->effectiveStiffness()[i](0, 0),
-                                   bd->effectiveCompliance()[i](0, 0)});
-        } else if (auto *mb = dynamic_cast<const MembraneStvkEnergy *>(e)) {
-            type = SPGX_ENERGY_MEMBRANE_STVK;
-            if (!mb->prepared()) throw std::runtime_error("MembraneStvkEnergy used before preparePrecomputations");
-            for (int i = 0; i < mb->nStencils(); ++i) {
-                const auto &D = mb->inverseReferenceMats()[i];
-                p.insert(p.end(), D.m, D.m + 4);
-                const auto &K = mb->effectiveStiffness()[i];
-                p.insert(p.end(), K.m, K.m + 9);
-                const auto &Cm = mb->effectiveCompliance()[i];
-                p.insert(p.end(), Cm.m, Cm.m + 9);
-            }
-        } else if (auto *sn = dynamic_cast<const StableNeoHookeanEnergy *>(e)) {
-            type = SPGX_ENERGY_STABLE_NEO_HOOKEAN;
-            if (!sn->prepared()) throw std::runtime_error("StableNeoHookeanEnergy used before preparePrecomputations");
-            for (int i = 0; i < sn->nStencils(); ++i) {
-                const auto &D = sn->inverseReferenceMats()[i];
-                p.insert(p.end(), D.m, D.m + 9);
-                p.insert(p.end(), {sn->effectiveStiffness()[i](0, 0), sn->effectiveStiffness()[i](1, 1),
-                                   sn->hydrostaticCorrectionTerms()[i], sn->effectiveCompliance()[i](0, 0),
-                                   sn->effectiveCompliance()[i](1, 1)});
-            }
-        } else {
-            throw std::runtime_error(std::string("energy type not supported by the GPU solver: ") + typeid(*e).name());
-        }
-        out.stencils.push_back(std::move(st));
-        out.params.push_back(std::move(p));
-        out.energies.push_back({type, e->nStencils(), nullptr, nullptr});
-    }
-    for (size_t k = 0; k < out.energies.size(); ++k) {
-        out.energies[k].stencils = out.stencils[k].data();
-        out.energies[k].params = out.params[k].data();
-    }
-    out.desc = {nv, out.x.data(), out.v.data(), out.mass.data(), static_cast<int32_t>(out.energies.size()),
-                out.energies.data()};
-}
-
-void pack(const std::vector<ParticleGroup> &groups, PackedScene &out)
-{
-    out.objects.clear();
-    out.objects.resize(groups.size());
-    out.descs.clear();
-    for (size_t i = 0; i < groups.size(); ++i) {
-        pack(groups[i], out.objects[i]);
-        out.descs.push_back(out.objects[i].desc);
-    }
-    out.desc = {static_cast<int32_t>(out.descs.size()), out.descs.data()};
-}
-
-}  // namespace spg::gpu
 
 namespace spg::solver {
 

@@ -14,8 +14,14 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libspgx.so")
 
 SPRING, ANCHOR, BENDING, STVK, SNH = 1, 2, 3, 4, 5
-STENCIL_SIZE = {SPRING: 2, ANCHOR: 1, BENDING: 4, STVK: 3, SNH: 4}
-PARAM_COUNT = {SPRING: 3, ANCHOR: 5, BENDING: 3, STVK: 22, SNH: 14}
+# Types 6-14: StVK tet, stable squared neo-Hookean, Baraff-Witkin membrane, Choi membrane,
+# Baraff-Witkin bending, quadratic bending, continuum spring, squared continuum spring, load.
+(STVK_TET, SSNH, BW_MEMBRANE, CHOI_MEMBRANE, BW_BENDING, QUAD_BENDING, SPRING_CONT, SPRING_SQ_CONT,
+ STATIC_LOAD) = range(6, 15)
+STENCIL_SIZE = {SPRING: 2, ANCHOR: 1, BENDING: 4, STVK: 3, SNH: 4, STVK_TET: 4, SSNH: 4, BW_MEMBRANE: 3,
+                CHOI_MEMBRANE: 3, BW_BENDING: 4, QUAD_BENDING: 4, SPRING_CONT: 2, SPRING_SQ_CONT: 2, STATIC_LOAD: 1}
+PARAM_COUNT = {SPRING: 3, ANCHOR: 5, BENDING: 3, STVK: 22, SNH: 14, STVK_TET: 13, SSNH: 13, BW_MEMBRANE: 10,
+               CHOI_MEMBRANE: 12, BW_BENDING: 3, QUAD_BENDING: 6, SPRING_CONT: 3, SPRING_SQ_CONT: 3, STATIC_LOAD: 4}
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "UNSUPPORTED_ENERGY", 3: "CUDA", 4: "NONFINITE", 5: "TIMEOUT",
           6: "NO_DEVICE"}

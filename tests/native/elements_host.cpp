@@ -3,13 +3,19 @@
 // against the oracle's automatic differentiation without a GPU. The shipped library never
 // calls this; its GPU kernels instantiate the same templates in FP32.
 #include "elements.cuh"
+#include "generic.cuh"
 
+#include <cmath>
 #include <cstdint>
 
 using namespace spgx;
 
 namespace {
-int ssize(int type) { return type == 1 ? 2 : type == 2 ? 1 : type == 3 ? 4 : type == 4 ? 3 : type == 5 ? 4 : 0; }
+int ssize(int type)
+{
+    static const int kSize[15] = {0, 2, 1, 4, 3, 4, 4, 4, 3, 3, 4, 4, 2, 2, 1};
+    return type >= 1 && type <= 14 ? kSize[type] : 0;
+}
 
 template <typename T>
 void eval_block(int type, const double *X, const double *p, int slot, double *g, double *H)
@@ -34,6 +40,15 @@ void eval_block(int type, const double *X, const double *p, int slot, double *g,
         T D[9];
         for (int i = 0; i < 9; ++i) D[i] = T(p[i]);
         snh_block(x, slot, D, T(p[9]), T(p[10]), T(p[11]), b);
+        break;
+    }
+    default: {  // types 6-14: the per-vertex forward-mode path, on positions relative to the vertex
+        static const int kParams[15] = {0, 3, 5, 3, 22, 14, 13, 13, 10, 12, 3, 6, 3, 3, 4};
+        T prm[13] = {};
+        for (int i = 0; i < kParams[type]; ++i) prm[i] = T(p[i]);
+        Vec3<T> r[4];
+        for (int j = 0; j < 4; ++j) r[j] = j < S ? x[j] - x[slot] : mk(T(0), T(0), T(0));
+        generic_block(type, r, slot, prm, b);
         break;
     }
     }

@@ -88,7 +88,7 @@ def test_validation_errors():
     bad_index = O.SceneObject(np.zeros((3, 3)), np.ones(3), [E(O.SPRING, np.array([[0, 3]], np.int32), np.ones((1, 3)))])
     with pytest.raises(N.SpgxError, match="invalid vertex"):
         N.color_vertices(bad_index)
-    bad_type = O.SceneObject(np.zeros((3, 3)), np.ones(3), [E(9, np.array([[0, 1]], np.int32), np.ones((1, 3)))])
+    bad_type = O.SceneObject(np.zeros((3, 3)), np.ones(3), [E(99, np.array([[0, 1]], np.int32), np.ones((1, 3)))])
     with pytest.raises(N.SpgxError):
         N.color_vertices(bad_type)
     with pytest.raises(N.SpgxError):
