@@ -85,6 +85,30 @@ static void inverse3x3(const double *A, double *Ai)
     Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
 }
 
+// n x n inverse by Gauss-Jordan elimination with partial pivoting (Eigen's inverse() for the
+// 4x4 XPBD system of the Choi membrane).
+static void inverse_gauss_jordan(const double *A, double *Ai, int n)
+{
+    double M[4][8];
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < 2 * n; ++c) M[r][c] = c < n ? A[r * n + c] : (c - n == r ? 1.0 : 0.0);
+    for (int k = 0; k < n; ++k) {
+        int piv = k;
+        for (int r = k + 1; r < n; ++r)
+            if (std::fabs(M[r][k]) > std::fabs(M[piv][k])) piv = r;
+        for (int c = 0; c < 2 * n; ++c) std::swap(M[k][c], M[piv][c]);
+        const double ip = 1.0 / M[k][k];
+        for (int c = 0; c < 2 * n; ++c) M[k][c] *= ip;
+        for (int r = 0; r < n; ++r)
+            if (r != k) {
+                const double f = M[r][k];
+                for (int c = 0; c < 2 * n; ++c) M[r][c] -= f * M[k][c];
+            }
+    }
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < n; ++c) Ai[r * n + c] = M[r][n + c];
+}
+
 static void inverse2x2(const double *A, double *Ai)
 {
     const double det = A[0] * A[3] - A[1] * A[2];
@@ -1030,11 +1054,18 @@ struct Xpbd {
         const double *params = &E.params[P * i];
         V3<double> p[4];
         for (int j = 0; j < S; ++j) p[j] = V3<double>(obj.x[3 * st[j]], obj.x[3 * st[j] + 1], obj.x[3 * st[j] + 2]);
-        double C[3], gradC[3 * 12];
+        double C[4], gradC[4 * 12];
         element_constraints(E.type, p, params, C, gradC);
         // Effective compliance matrix (NC x NC)
-        double cmp[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        if (E.type == kStvk) {
+        double cmp[16] = {};
+        if (E.type >= kStvkTet) {  // diagonal compliances of types 6-13 (parameter layouts above)
+            const int off = (E.type == kStvkTet || E.type == kSsnh) ? 11
+                            : E.type == kBwMembrane                 ? 7
+                            : E.type == kChoi                       ? 8
+                            : E.type == kQuadBending                ? 5
+                                                                    : 2;
+            for (int c = 0; c < NC; ++c) cmp[c * NC + c] = params[E.type == kQuadBending ? off : off + c];
+        } else if (E.type == kStvk) {
             for (int k = 0; k < 9; ++k) cmp[k] = params[13 + k];
         } else if (E.type == kSnh) {
             cmp[0] = params[12];
@@ -1047,25 +1078,27 @@ struct Xpbd {
             cmp[0] = params[2];
         }
         // WgradC and A = gradC^T W gradC + cmp / dt^2 + 1e-10 I
-        double WgradC[3 * 12];
+        double WgradC[4 * 12];
         for (int c = 0; c < NC; ++c)
             for (int j = 0; j < S; ++j)
                 for (int a = 0; a < 3; ++a) WgradC[c * 3 * S + 3 * j + a] = obj.w[st[j]] * gradC[c * 3 * S + 3 * j + a];
-        double A[9];
+        double A[16];
         for (int r = 0; r < NC; ++r)
             for (int c = 0; c < NC; ++c) {
                 double acc = 0;
                 for (int d = 0; d < 3 * S; ++d) acc += gradC[r * 3 * S + d] * WgradC[c * 3 * S + d];
                 A[r * NC + c] = acc + cmp[r * NC + c] / (h * h) + (r == c ? 1e-10 : 0.0);
             }
-        double Ai[9];
+        double Ai[16];
         if (NC == 1)
             Ai[0] = 1.0 / A[0];
         else if (NC == 2)
             inverse2x2(A, Ai);
-        else
+        else if (NC == 3)
             inverse3x3(A, Ai);
-        double dl[3];
+        else
+            inverse_gauss_jordan(A, Ai, NC);
+        double dl[4];
         for (int r = 0; r < NC; ++r) {
             double acc = 0;
             for (int c = 0; c < NC; ++c) acc += Ai[r * NC + c] * C[c];

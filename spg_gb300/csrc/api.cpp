@@ -29,7 +29,15 @@ int32_t spgx_num_constraints(int32_t type)
     case SPGX_ENERGY_SPRING:
     case SPGX_ENERGY_SPRING_ANCHOR:
     case SPGX_ENERGY_DISCRETE_BENDING: return 1;
-    default: return 0;
+    case SPGX_ENERGY_STVK:
+    case SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN: return 2;
+    case SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN: return 3;
+    case SPGX_ENERGY_MEMBRANE_CHOI: return 4;
+    case SPGX_ENERGY_BARAFF_WITKIN_BENDING: return 1;
+    case SPGX_ENERGY_QUADRATIC_BENDING: return 3;
+    case SPGX_ENERGY_SPRING_CONTINUUM:
+    case SPGX_ENERGY_SPRING_SQUARED_CONTINUUM: return 1;
+    default: return 0;  // including the static load, which has no constraint form
     }
 }
 

@@ -74,8 +74,8 @@ __global__ void eval_constraints_kernel(int type, int n, int S, int P, int NC, c
     const float *p = prm + size_t(i) * P;
     V3f r[4];
     for (int j = 0; j < S; ++j) r[j] = mk(x[3 * j] - x[0], x[3 * j + 1] - x[1], x[3 * j + 2] - x[2]);
-    float c[3] = {0.f, 0.f, 0.f};
-    V3f g[12];
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    V3f g[16];
     switch (type) {
     case SPGX_ENERGY_SPRING: {
         const V3f s = r[0] - r[1];
@@ -94,10 +94,23 @@ __global__ void eval_constraints_kernel(int type, int n, int S, int P, int NC, c
         stvk_constraints(r, D, c, g);
         break;
     }
-    default: {
+    case SPGX_ENERGY_STABLE_NEO_HOOKEAN: {
         float D[9];
         for (int k = 0; k < 9; ++k) D[k] = p[k];
         snh_constraints(r, D, p[11], c, g);
+        break;
+    }
+    default: {  // types 6-13: per-vertex forward mode, one stencil vertex at a time
+        V3f q[4];
+        for (int j = 0; j < 4; ++j) q[j] = j < S ? r[j] : mk(0.f, 0.f, 0.f);
+        for (int j = 0; j < S; ++j) {
+            VAD<float> cv[4];
+            const int nc = generic_constraints(type, q, j, p, cv);
+            for (int k = 0; k < nc; ++k) {
+                c[k] = cv[k].v;
+                g[k * S + j] = mk(cv[k].g[0], cv[k].g[1], cv[k].g[2]);
+            }
+        }
         break;
     }
     }

@@ -344,6 +344,108 @@ SPGX_HD void static_load_block(const T *prm, Block<T> &b)
     sub_force(b, d, -prm[0]);
 }
 
+// Constraints of types 6-13 (the reference's dConstraints lambdas, cited above; the StVK tet's
+// is [tr G, sqrt(2 tr(G G))], stvkEnergy.cpp:9-35, with the second set to 0 when its value
+// is 0), differentiated with respect to the vertex at `slot`. Returns their number (0 for the
+// static load, which has no constraint form: staticLoadEnergy.cpp:8-15).
+template <typename T>
+SPGX_HD int generic_constraints(int type, const Vec3<T> *p, int slot, const T *prm, VAD<T> *C)
+{
+    switch (type) {
+    case SPGX_ENERGY_STVK: {
+        V3A<T> q[4], f[3];
+        seed_positions<T, 4>(p, slot, q);
+        deformation_columns<T, 3>(q, prm, f);
+        VAD<T> tr = vconst(T(0)), sq = vconst(T(0));
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                VAD<T> G = T(0.5) * vdot(f[a], f[c]);
+                if (a == c) G = G + T(-0.5);
+                if (a == c) tr = tr + G;
+                sq = sq + G * G;
+            }
+        C[0] = tr;
+        C[1] = sq.v == T(0) ? vconst(T(0)) : vsqrt(T(2) * sq);
+        return 2;
+    }
+    case SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN: {
+        V3A<T> q[4], f[3];
+        seed_positions<T, 4>(p, slot, q);
+        deformation_columns<T, 3>(q, prm, f);
+        C[0] = vdot(f[0], vcross(f[1], f[2])) + T(-1);
+        C[1] = vdot(f[0], f[0]) + vdot(f[1], f[1]) + vdot(f[2], f[2]) + T(-3);
+        return 2;
+    }
+    case SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN:
+    case SPGX_ENERGY_MEMBRANE_CHOI: {
+        V3A<T> q[3], f[2];
+        seed_positions<T, 3>(p, slot, q);
+        deformation_columns<T, 2>(q, prm, f);
+        C[0] = vnorm(f[0]) + T(-1);
+        C[1] = vnorm(f[1]) + T(-1);
+        if (type == SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN) {
+            C[2] = vdot(f[0], f[1]);
+            return 3;
+        }
+        const T s = T(0.70710678118654752440);
+        C[2] = vnorm(vscale(s, vadd(f[0], f[1]))) + T(-1);
+        C[3] = vnorm(vscale(s, vsub(f[0], f[1]))) + T(-1);
+        return 4;
+    }
+    case SPGX_ENERGY_BARAFF_WITKIN_BENDING: {
+        V3A<T> q[4];
+        seed_positions<T, 4>(p, slot, q);
+        const V3A<T> e0 = vsub(q[1], q[0]), e3 = vsub(q[2], q[1]), e4 = vsub(q[3], q[1]);
+        const T e0i = T(1) / sqrt(vdot(e0, e0).v);
+        const V3A<T> n1 = vcross(e0, e3);
+        const V3A<T> n2 = vscale(T(-1), vcross(e0, e4));
+        const T n1i = T(1) / sqrt(vdot(n1, n1).v);
+        const T n2i = T(1) / sqrt(vdot(n2, n2).v);
+        const V3A<T> a = vscale(n1i, n1), c = vscale(n2i, n2);
+        C[0] = vatan2(vdot(vcross(a, c), vscale(e0i, e0)), vdot(a, c)) + (-prm[0]);
+        return 1;
+    }
+    case SPGX_ENERGY_QUADRATIC_BENDING: {
+        V3A<T> q[4];
+        seed_positions<T, 4>(p, slot, q);
+        V3A<T> s = vscale(prm[0], q[0]);
+#pragma unroll
+        for (int j = 1; j < 4; ++j) s = vadd(s, vscale(prm[j], q[j]));
+        C[0] = s.x;
+        C[1] = s.y;
+        C[2] = s.z;
+        return 3;
+    }
+    case SPGX_ENERGY_SPRING_CONTINUUM:
+    case SPGX_ENERGY_SPRING_SQUARED_CONTINUUM: {
+        V3A<T> q[2];
+        seed_positions<T, 2>(p, slot, q);
+        const V3A<T> d = vsub(q[0], q[1]);
+        const T L0 = prm[0];
+        C[0] = type == SPGX_ENERGY_SPRING_SQUARED_CONTINUUM ? (T(1) / (L0 * L0)) * vdot(d, d) + T(-1)
+                                                            : (T(1) / L0) * vnorm(d) + T(-1);
+        return 1;
+    }
+    default: return 0;
+    }
+}
+
+// Effective compliance diagonal of a type-6..13 element (parameter layouts in spgx.h).
+template <typename T>
+SPGX_HD T generic_compliance(int type, const T *prm, int c)
+{
+    switch (type) {
+    case SPGX_ENERGY_STVK:
+    case SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN: return prm[11 + c];
+    case SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN: return prm[7 + c];
+    case SPGX_ENERGY_MEMBRANE_CHOI: return prm[8 + c];
+    case SPGX_ENERGY_QUADRATIC_BENDING: return prm[5];
+    default: return prm[2];  // Baraff-Witkin bending, continuum springs
+    }
+}
+
 // The block of one incidence of a type-6..14 energy at stencil positions p (relative to the
 // solved vertex, p[slot] = 0).
 template <typename T>

@@ -19,9 +19,11 @@
 namespace spgx {
 
 // Work item: (type << 28) | element index in the type's table (types 1..5 keep the item
-// non-negative; tables are limited to 2^28 elements).
+// non-negative; tables are limited to 2^28 elements). Energies of types 6-13 share the tag
+// kItemGeneric and index the generic element table.
 constexpr int kItemShift = 28;
 constexpr int kItemMask = (1 << kItemShift) - 1;
+constexpr int kItemGeneric = 6;
 
 __device__ __forceinline__ void add_delta(float4 *pos, int v, V3f dx)
 {
@@ -50,6 +52,32 @@ __device__ __forceinline__ void project_block(float4 *pos, const int *idx, const
     float dl[NC];
     if (NC == 1) {
         dl[0] = -C[0] / A[0][0];
+    } else if (NC == 4) {
+        // Gaussian elimination (A is symmetric positive definite plus the compliance).
+        float M[NC][NC + 1];
+#pragma unroll
+        for (int r = 0; r < NC; ++r) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) M[r][c] = A[r][c];
+            M[r][NC] = -C[r];
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float ip = 1.f / M[k][k];
+#pragma unroll
+            for (int r = k + 1; r < NC; ++r) {
+                const float f = M[r][k] * ip;
+#pragma unroll
+                for (int c = k; c <= NC; ++c) M[r][c] -= f * M[k][c];
+            }
+        }
+#pragma unroll
+        for (int k = NC - 1; k >= 0; --k) {
+            float acc = M[k][NC];
+#pragma unroll
+            for (int c = k + 1; c < NC; ++c) acc -= M[k][c] * dl[c];
+            dl[k] = acc / M[k][k];
+        }
     } else if (NC == 2) {
         const float det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
         dl[0] = -(A[1][1] * C[0] - A[0][1] * C[1]) / det;
@@ -79,6 +107,60 @@ __device__ __forceinline__ void project_block(float4 *pos, const int *idx, const
     }
 }
 
+// StencilBlockEnergy::projectPosition (energy.h:117-153) for the energies of types 6-13: the
+// constraint gradients with respect to each stencil vertex come from the per-vertex
+// forward-mode evaluation, one vertex at a time.
+template <int S, int NC>
+__device__ __forceinline__ void xpbd_generic_project(float4 *pos, const int *idx, const float *w, int type,
+                                                     const V3f *p, const float *prm, float invh2)
+{
+    float C[NC];
+    V3f g[NC * S];
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+        VAD<float> c[4];
+        generic_constraints(type, p, j, prm, c);
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            g[k * S + j] = mk(c[k].g[0], c[k].g[1], c[k].g[2]);
+            if (j == 0) C[k] = c[k].v;
+        }
+    }
+    float cmp[NC * NC];
+#pragma unroll
+    for (int r = 0; r < NC; ++r)
+#pragma unroll
+        for (int c = 0; c < NC; ++c) cmp[r * NC + c] = r == c ? generic_compliance(type, prm, r) : 0.f;
+    project_block<S, NC>(pos, idx, w, C, g, cmp, invh2);
+}
+
+__device__ __noinline__ void xpbd_generic(const DevTables &T, float4 *pos, const float *__restrict__ invm, int e,
+                                          float invh2)
+{
+    const int4 ix = __ldg(T.gen_idx + e);
+    const int4 info = __ldg(T.gen_info + e);
+    const int type = info.x, S = info.z;
+    const float *prm = T.gen_prm + info.y;
+    const int idx[4] = {ix.x, ix.y, ix.z, ix.w};
+    const V3f b0 = v3(pos[2 * ix.x]), d0 = v3(pos[2 * ix.x + 1]);
+    V3f p[4];
+    float w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        p[j] = (j == 0 || j >= S) ? mk(0.f, 0.f, 0.f) : (v3(pos[2 * idx[j]]) - b0) + (v3(pos[2 * idx[j] + 1]) - d0);
+        w[j] = j < S ? __ldg(invm + idx[j]) : 0.f;
+    }
+    switch (type) {
+    case SPGX_ENERGY_STVK:
+    case SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN: xpbd_generic_project<4, 2>(pos, idx, w, type, p, prm, invh2); break;
+    case SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN: xpbd_generic_project<3, 3>(pos, idx, w, type, p, prm, invh2); break;
+    case SPGX_ENERGY_MEMBRANE_CHOI: xpbd_generic_project<3, 4>(pos, idx, w, type, p, prm, invh2); break;
+    case SPGX_ENERGY_BARAFF_WITKIN_BENDING: xpbd_generic_project<4, 1>(pos, idx, w, type, p, prm, invh2); break;
+    case SPGX_ENERGY_QUADRATIC_BENDING: xpbd_generic_project<4, 3>(pos, idx, w, type, p, prm, invh2); break;
+    default: xpbd_generic_project<2, 1>(pos, idx, w, type, p, prm, invh2); break;  // continuum springs
+    }
+}
+
 __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, float4 *pos, const float *__restrict__ invm,
                                                          const int *__restrict__ items, int n, float invh2)
 {
@@ -87,6 +169,10 @@ __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, floa
     const int item = __ldg(items + t);
     const int type = (item >> kItemShift) & 7;
     const int e = item & kItemMask;
+    if (type == kItemGeneric) {
+        xpbd_generic(T, pos, invm, e, invh2);
+        return;
+    }
     switch (type) {
     case SPGX_ENERGY_SPRING: {
         // SpringEnergy::projectPosition, springEnergy.cpp:48-68
@@ -243,10 +329,12 @@ struct XpbdSolver {
             set_error(err);
             return st;
         }
-        if (!L.gen_idx_empty()) {
-            set_error("the XPBD solver supports energy types 1-5 only");
-            return SPGX_ERR_UNSUPPORTED_ENERGY;
-        }
+        for (const auto &O : L.objects)
+            for (int t : O.energy_types)
+                if (t == SPGX_ENERGY_STATIC_LOAD) {  // the reference throws too (staticLoadEnergy.cpp:8-15)
+                    set_error("Constraint-based load energy not implemented");
+                    return SPGX_ERR_UNSUPPORTED_ENERGY;
+                }
         SPGX_TRY_STATUS(check_params(params));
         P = *params;
         h_sub = P.dt / P.substeps;
@@ -258,10 +346,11 @@ struct XpbdSolver {
         SPGX_CUDA(cudaEventCreate(&ev1));
         SPGX_TRY_STATUS(X.init(L));
         SPGX_TRY_STATUS(EB.upload(L.el, T));
+        SPGX_TRY_STATUS(EB.upload_generic(L, T));
         SPGX_TRY_STATUS(d_anchor_v.upload(L.el.anchor_v));
         const size_t cap = size_t(1) << kItemShift;
         if (L.el.anchors.size() >= cap || L.el.springs.size() >= cap || L.el.bend_idx.size() >= cap ||
-            L.el.stvk_idx.size() >= cap || L.el.snh_idx.size() >= cap) {
+            L.el.stvk_idx.size() >= cap || L.el.snh_idx.size() >= cap || L.el.gen_idx.size() >= cap) {
             set_error("XPBD supports at most 2^28 stencils per energy type");
             return SPGX_ERR_INVALID_ARG;
         }
@@ -285,7 +374,9 @@ struct XpbdSolver {
                         if ((type == SPGX_ENERGY_SPRING_ANCHOR) != (anch == 1)) continue;
                         const auto &cols = O.stencil_colors[k];
                         for (int s = 0; s < static_cast<int>(cols.size()); ++s)
-                            if (cols[s] == c) items.push_back((type << kItemShift) | (L.elem_base[o][k] + s));
+                            if (cols[s] == c)
+                                items.push_back(((is_generic_type(type) ? kItemGeneric : type) << kItemShift) |
+                                                (L.elem_base[o][k] + s));
                     }
                     ph.count = static_cast<int>(items.size()) - ph.offset;
                     if (ph.count > 0) phases.push_back(ph);

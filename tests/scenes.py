@@ -158,14 +158,17 @@ def cloth_variant(kind, rows=9):
 
 def spring_variant(n=9, load=True):
     """The spring cloth's edges as continuum springs (12) and squared continuum springs (13)
-    of half the stiffness each, its anchors, and a static load (14) on the bottom row."""
+    whose small-strain stiffnesses (k / L0 and 4 k / L0) are each about half the spring
+    cloth's 1e4 N/m, its anchors, and a static load (14) about the vertex weight on the
+    bottom row."""
     s = spring_cloth_cfg3(n)
     pairs = next(e for e in s.energies if e.type == O.SPRING).stencils
-    energies = [_energy(O.SPRING_CONT, pairs, continuum_spring_params(s.x0, pairs, 5e3)),
-                _energy(O.SPRING_SQ_CONT, pairs, continuum_spring_params(s.x0, pairs, 5e3))]
+    energies = [_energy(O.SPRING_CONT, pairs, continuum_spring_params(s.x0, pairs, 20.0)),
+                _energy(O.SPRING_SQ_CONT, pairs, continuum_spring_params(s.x0, pairs, 5.0))]
     energies += [e for e in s.energies if e.type == O.ANCHOR]
     if load:
         bottom = np.arange((n - 1) * n, n * n, dtype=np.int32).reshape(-1, 1)
         d = np.array([0.0, 0.6, 0.8])
-        energies.append(_energy(O.STATIC_LOAD, bottom, np.tile(np.concatenate([[1e-3], d]), (n, 1))))
+        weight = float(s.mass.max()) * 9.81
+        energies.append(_energy(O.STATIC_LOAD, bottom, np.tile(np.concatenate([[weight], d]), (n, 1))))
     return O.SceneObject(s.x.copy(), s.mass.copy(), energies, None, s.x0.copy())

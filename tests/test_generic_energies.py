@@ -164,11 +164,62 @@ def test_positions_after_10_steps_match_oracle(name):
 
 
 @pytest.mark.gpu
-def test_tile_kernels_and_xpbd_refuse_these_energies():
+def test_tile_kernels_refuse_these_energies_and_xpbd_the_load():
     N = pytest.importorskip("spg_gb300.native")
     obj = _variant_scenes()["bw"]
     for k in (2, 3):
         with pytest.raises(N.SpgxError):
             N.VbdSolver([obj], dt=1 / 60, iterations=5, gravity=scenes.GRAVITY, kernel=k)
-    with pytest.raises(N.SpgxError):
-        N.XpbdSolver([obj], dt=1 / 60, substeps=2, gravity=scenes.GRAVITY)
+    with pytest.raises(N.SpgxError, match="load"):
+        N.XpbdSolver([scenes.spring_variant(load=True)], dt=1 / 60, substeps=2, gravity=scenes.GRAVITY)
+
+
+def _xpbd_scenes():
+    v = _variant_scenes()
+    v["springs"] = scenes.spring_variant(load=False)
+    del v["springs_load"]
+    return v
+
+
+def test_oracle_xpbd_steps_the_variant_scenes():
+    for name, obj in _xpbd_scenes().items():
+        s = O.Xpbd(obj, 1 / 60, 4, scenes.GRAVITY)
+        for _ in range(3):
+            s.step()
+        x, _ = s.state()
+        assert np.all(np.isfinite(x)), name
+
+
+@pytest.mark.gpu
+def test_device_constraints_match_oracle():
+    N = pytest.importorskip("spg_gb300.native")
+    by_type = {}
+    for etype, X, p, slot in _cases():
+        if etype != O.STATIC_LOAD and slot == 0:
+            by_type.setdefault(etype, []).append((X, p))
+    for etype, rows in by_type.items():
+        X = np.array([r[0] for r in rows]).astype(np.float32).astype(np.float64)
+        P = np.array([r[1] for r in rows]).astype(np.float32).astype(np.float64)
+        c, g = N.eval_constraints(etype, X, P)
+        for i in range(len(rows)):
+            cr, gr = O.element_constraints(etype, X[i], P[i])
+            assert np.abs(c[i] - cr).max() <= 1e-4 * max(1.0, np.abs(cr).max()), etype
+            assert np.abs(g[i] - gr).max() <= 1e-4 * max(1.0, np.abs(gr).max()), etype
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["stvk_tet", "ssnh", "bw", "choi_quad", "springs"])
+def test_xpbd_positions_match_oracle(name):
+    N = pytest.importorskip("spg_gb300.native")
+    obj = _xpbd_scenes()[name]
+    gpu = N.XpbdSolver([obj], dt=1 / 60, substeps=8, gravity=scenes.GRAVITY)
+    ref = O.Xpbd(obj, 1 / 60, 8, scenes.GRAVITY)
+    for _ in range(10):
+        gpu.step()
+        ref.step()
+    xg, _ = gpu.state(0)
+    xr, _ = ref.state()
+    extent = float(np.ptp(obj.x0, axis=0).max())
+    err = np.abs(xg - xr).max()
+    print(f"XPBD {name}: max |dx| after 10 steps {err:.3g} m (extent {extent:.3g} m)")
+    assert err <= 1e-4 * extent
