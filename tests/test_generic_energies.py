@@ -18,10 +18,10 @@ dp = C.POINTER(C.c_double)
 
 
 def _variant_scenes():
-    return {"stvk_tet": scenes.beam_tet_variant(O.STVK_TET), "ssnh": scenes.beam_tet_variant(O.SSNH),
+    return {"stvk_tet_load": scenes.beam_tet_variant(O.STVK_TET, load=True), "ssnh": scenes.beam_tet_variant(O.SSNH),
             "bw": scenes.cloth_variant((O.BW_MEMBRANE, O.BW_BENDING)),
             "choi_quad": scenes.cloth_variant((O.CHOI_MEMBRANE, O.QUAD_BENDING)),
-            "springs_load": scenes.spring_variant()}
+            "springs": scenes.spring_variant()}
 
 
 def _cases(n_per_energy=12, seed=3):
@@ -144,7 +144,7 @@ def test_device_blocks_match_oracle():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["stvk_tet", "ssnh", "bw", "choi_quad", "springs_load"])
+@pytest.mark.parametrize("name", ["stvk_tet_load", "ssnh", "bw", "choi_quad", "springs"])
 def test_positions_after_10_steps_match_oracle(name):
     N = pytest.importorskip("spg_gb300.native")
     obj = _variant_scenes()[name]
@@ -176,8 +176,8 @@ def test_tile_kernels_refuse_these_energies_and_xpbd_the_load():
 
 def _xpbd_scenes():
     v = _variant_scenes()
-    v["springs"] = scenes.spring_variant(load=False)
-    del v["springs_load"]
+    v["stvk_tet"] = scenes.beam_tet_variant(O.STVK_TET)
+    del v["stvk_tet_load"]
     return v
 
 

@@ -127,7 +127,7 @@ def _patch(n=17):
 @pytest.mark.gpu
 def test_zero_network_equals_the_extrapolated_guess():
     """The network only corrects the extrapolated guess: with zero weights the learned mode
-    proposes exactly that guess, so its trajectory equals mode 2's bit for bit."""
+    proposes exactly that guess (x_e + l * 0), so its trajectory equals mode 2's bit for bit."""
     obj = _patch()
     kw = dict(dt=1 / 120, iterations=10, gravity=(0, 0, -9.81))
     ext = N.VbdSolver([obj], **kw)
@@ -138,8 +138,9 @@ def test_zero_network_equals_the_extrapolated_guess():
     for _ in range(4):
         a = ext.step()
         b = warm.step()
-        assert b.warm_accepted == 0  # ties keep the simpler guess
-        assert a.extrapolated_accepted == b.extrapolated_accepted
+        # The two candidates are the same positions; their FP64 residual sums may differ in
+        # the last bits (atomic order), so either may be the one counted.
+        assert a.extrapolated_accepted == b.extrapolated_accepted + b.warm_accepted
     assert np.array_equal(ext.state(0)[0], warm.state(0)[0])
 
 
