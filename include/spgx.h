@@ -12,6 +12,8 @@
  *                                   spg/source/sim/solver/vbd.cpp:12-268
  *   spgx_xpbd_*  spg::solver::XPBD  spg/include/spg/sim/solver/xpbd.h:13-27,
  *                                   spg/source/sim/solver/xpbd.cpp:16-160
+ *   spgx_implicit_*  spg::solver::ImplicitEulerNewtonDx  implicitEulerNewtonDx.cpp:11-65,
+ *                                   implicitEulerBase.cpp:102-240
  *   spgx_energy_desc   the five Energy<ParticleGroup> implementations on the hot path and
  *                      their precomputed per-stencil data (energy.h:21-369)
  *
@@ -311,6 +313,36 @@ spgx_status spgx_eval_vertex_blocks_noalloc(int32_t type, int32_t n, const doubl
 spgx_status spgx_eval_constraints(int32_t type, int32_t n, const double *X, const double *params, double *C,
                                   double *gradC);
 int32_t spgx_num_constraints(int32_t type);
+
+/* ------------------------------------------------------------------------------------ */
+/* Implicit Euler, one Newton step per substep (spg::solver::ImplicitEulerNewtonDx,
+ * implicitEulerNewtonDx.cpp:11-65, with ImplicitEulerBase's system force, stiffness matrix
+ * and conjugate-gradient solve, implicitEulerBase.cpp:102-240). Per substep: y = x + h v,
+ * f = M g - grad E(y), solve (M / h^2 + hess E(y)) dx = f by conjugate gradients with the
+ * diagonal preconditioner, x = y + dx, v = (x - x0) / h. Every energy type is accepted; the
+ * element Hessians are the full ones (no definiteness projection), as in the reference.
+ * spgx_step_stats: iterations = CG iterations summed over substeps, residual_final = the
+ * last solve's relative residual |r| / |f|, converged = every solve reached cg_threshold. */
+
+typedef struct spgx_implicit spgx_implicit;
+
+typedef struct spgx_implicit_params {
+    double dt;                 /* BaseSolver::setDt */
+    int32_t substeps;          /* BaseSolver::setNumSubsteps */
+    double gravity[3];         /* BaseSolver::setGravity */
+    double cg_threshold;       /* ImplicitEulerBase::m_cgThreshold (1e-5) */
+    int32_t cg_max_iterations; /* ImplicitEulerBase::m_cgMaxIterations (300) */
+    int32_t device;
+} spgx_implicit_params;
+
+void spgx_implicit_params_default(spgx_implicit_params *p);
+spgx_status spgx_implicit_create(const spgx_scene_desc *scene, const spgx_implicit_params *params,
+                                 spgx_implicit **out);
+spgx_status spgx_implicit_destroy(spgx_implicit *h);
+spgx_status spgx_implicit_step(spgx_implicit *h, spgx_step_stats *stats);
+spgx_status spgx_implicit_get_state(spgx_implicit *h, int32_t object, double *x, double *v);
+spgx_status spgx_implicit_set_state(spgx_implicit *h, int32_t object, const double *x, const double *v);
+spgx_status spgx_implicit_reset(spgx_implicit *h);
 
 /* ------------------------------------------------------------------------------------ */
 /* XPBD (one projection sweep per substep, xpbd.h:13-15)                                  */

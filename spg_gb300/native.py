@@ -61,6 +61,11 @@ class XpbdParams(C.Structure):
                 ("block_size", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32)]
 
 
+class ImplicitParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("substeps", C.c_int32), ("gravity", C.c_double * 3),
+                ("cg_threshold", C.c_double), ("cg_max_iterations", C.c_int32), ("device", C.c_int32)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("fallback_solves", C.c_int32), ("skipped_solves", C.c_int32),
                 ("converged", C.c_int32), ("residual_initial", C.c_double), ("residual_final", C.c_double),
@@ -126,6 +131,13 @@ def lib():
         L.spgx_vbd_set_warm_start.argtypes = [vp, vp, i32]
         L.spgx_vbd_step_record.argtypes = [vp, fp, fp, C.POINTER(StepStats)]
         L.spgx_vbd_get_vertex_order.argtypes = [vp, ip]
+        L.spgx_implicit_params_default.argtypes = [C.POINTER(ImplicitParams)]
+        L.spgx_implicit_create.argtypes = [C.POINTER(SceneDesc), C.POINTER(ImplicitParams), C.POINTER(vp)]
+        L.spgx_implicit_destroy.argtypes = [vp]
+        L.spgx_implicit_step.argtypes = [vp, C.POINTER(StepStats)]
+        L.spgx_implicit_get_state.argtypes = [vp, i32, dp, dp]
+        L.spgx_implicit_set_state.argtypes = [vp, i32, dp, dp]
+        L.spgx_implicit_reset.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -347,6 +359,51 @@ class Mlp:
         check(lib().spgx_mlp_train(self.h, x.shape[0], _p(x, C.c_float), _p(y, C.c_float), steps, batch, lr, seed,
                                    C.byref(loss)))
         return loss.value
+
+
+class ImplicitSolver:
+    """Implicit Euler with one Newton step per substep (ImplicitEulerNewtonDx) on one GPU."""
+
+    def __init__(self, objects, dt=0.01, substeps=1, gravity=(0.0, -9.8, 0.0), cg_threshold=1e-5,
+                 cg_max_iterations=300, device=0):
+        self.objects_nv = [len(np.asarray(o.mass).reshape(-1)) for o in objects]
+        self._d = Descriptor(objects)
+        p = ImplicitParams()
+        lib().spgx_implicit_params_default(C.byref(p))
+        p.dt, p.substeps = dt, substeps
+        p.gravity = (C.c_double * 3)(*gravity)
+        p.cg_threshold, p.cg_max_iterations, p.device = cg_threshold, cg_max_iterations, device
+        self.params = p
+        h = C.c_void_p()
+        check(lib().spgx_implicit_create(C.byref(self._d.scene), C.byref(p), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().spgx_implicit_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def step(self) -> StepStats:
+        st = StepStats()
+        check(lib().spgx_implicit_step(self.h, C.byref(st)))
+        return st
+
+    def state(self, obj=0):
+        n = self.objects_nv[obj]
+        x = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        check(lib().spgx_implicit_get_state(self.h, obj, _p(x, C.c_double), _p(v, C.c_double)))
+        return x, v
+
+    def set_state(self, obj, x, v=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        check(lib().spgx_implicit_set_state(self.h, obj, _p(x, C.c_double), None if vv is None else _p(vv, C.c_double)))
+
+    def reset(self):
+        check(lib().spgx_implicit_reset(self.h))
 
 
 class XpbdSolver:
