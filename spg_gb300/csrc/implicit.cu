@@ -12,7 +12,10 @@
 // Layout: the global matrix is block-sparse with 3x3 blocks (BSR) over the vertex adjacency of
 // all stencils; one thread per element computes the element's gradient and Hessian blocks by
 // forward-mode differentiation over vertex pairs (6 seeded coordinates) and adds them with
-// atomics. Vectors are FP32, inner products FP64.
+// atomics. Assembly, parameters and the CG run in FP64 (the positions stay FP32 base + delta):
+// a flat cloth at rest has no transverse stiffness, and FP32 rounding of 1 - L0 / |x1 - x0|
+// would add some of the order of the M / h^2 term and change the solution. This solver is off
+// the VBD hot path, so FP64's lower rate is acceptable here.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,60 +32,66 @@
 namespace spgx {
 
 struct ImplicitTables {
-    const int4 *idx;    // per element: internal vertex ids (-1 padded)
-    const int4 *info;   // per element: {type, param offset, stencil size, 0}
-    const float *prm;   // parameters in the spgx.h layouts
-    const int *eblk;    // per element: S x S block positions in the BSR values (row-major)
+    const int4 *idx;     // per element: internal vertex ids (-1 padded)
+    const int4 *info;    // per element: {type, param offset, stencil size, 0}
+    const double *prm;   // parameters in the spgx.h layouts
+    const int *eblk;     // per element: S x S block positions in the BSR values (row-major)
     const int *row_ptr;  // BSR rows (internal vertices)
     const int *col;      // BSR block columns
-    float *val;          // BSR values, 9 per block (row-major)
+    double *val;         // BSR values, 9 per block (row-major)
     const int *diag;     // per vertex: position of its diagonal block
 };
 
-__device__ __forceinline__ void atomic_block(float *val, int blk, const float H[9])
+// Vectors over the vertices: 3 doubles per vertex.
+__device__ __forceinline__ void atomic_block(double *val, int blk, const double H[9])
 {
-    float *b = val + size_t(blk) * 9;
+    double *b = val + size_t(blk) * 9;
 #pragma unroll
     for (int k = 0; k < 9; ++k) atomicAdd(b + k, H[k]);
 }
 
-__device__ __forceinline__ void atomic_force(float4 *f, int v, float gx, float gy, float gz)
+__device__ __forceinline__ void atomic_force(double *f, int v, double gx, double gy, double gz)
 {
-    atomicAdd(&f[v].x, -gx);
-    atomicAdd(&f[v].y, -gy);
-    atomicAdd(&f[v].z, -gz);
+    atomicAdd(f + 3 * v, -gx);
+    atomicAdd(f + 3 * v + 1, -gy);
+    atomicAdd(f + 3 * v + 2, -gz);
+}
+
+// Position of vertex j relative to (b0, d0), in FP64 from the FP32 base/delta pairs.
+__device__ __forceinline__ Vec3<double> rel64(const float4 *pos, int j, float4 b0, float4 d0)
+{
+    const float4 b = pos[2 * j], d = pos[2 * j + 1];
+    return mk((double(b.x) - b0.x) + (double(d.x) - d0.x), (double(b.y) - b0.y) + (double(d.y) - d0.y),
+              (double(b.z) - b0.z) + (double(d.z) - d0.z));
 }
 
 // Gradient and Hessian blocks of one element at the current positions, added to the forces
 // (f -= grad) and to the matrix (val += hess).
 template <int S>
-__device__ void assemble_element(const ImplicitTables &T, const float4 *__restrict__ pos, float4 *force, int e,
+__device__ void assemble_element(const ImplicitTables &T, const float4 *__restrict__ pos, double *force, int e,
                                  int4 ix, int4 info)
 {
     const int iv[4] = {ix.x, ix.y, ix.z, ix.w};
-    const float *prm = T.prm + info.y;
+    const double *prm = T.prm + info.y;
     const int type = info.x;
     const int *eb = T.eblk + size_t(e) * 16;
     const float4 b0 = pos[2 * iv[0]], d0 = pos[2 * iv[0] + 1];
-    Vec3<float> p[S];
+    Vec3<double> p[S];
 #pragma unroll
-    for (int j = 0; j < S; ++j) {
-        const float4 b = pos[2 * iv[j]], d = pos[2 * iv[j] + 1];
-        p[j] = mk((b.x - b0.x) + (d.x - d0.x), (b.y - b0.y) + (d.y - d0.y), (b.z - b0.z) + (d.z - d0.z));
-    }
+    for (int j = 0; j < S; ++j) p[j] = rel64(pos, iv[j], b0, d0);
     if (type == SPGX_ENERGY_QUADRATIC_BENDING) {
         // C = sum_s c_s x_s (linear): grad_a = k c_a C, hess_ab = k c_a c_b I.
-        Vec3<float> C = mk(0.f, 0.f, 0.f);
+        Vec3<double> C = mk(0.0, 0.0, 0.0);
 #pragma unroll
         for (int s = 0; s < S; ++s) C = C + prm[s] * p[s];
-        const float k = prm[4];
+        const double k = prm[4];
 #pragma unroll
         for (int a = 0; a < S; ++a) {
             atomic_force(force, iv[a], k * prm[a] * C.x, k * prm[a] * C.y, k * prm[a] * C.z);
 #pragma unroll
             for (int b = 0; b < S; ++b) {
-                const float s = k * prm[a] * prm[b];
-                const float H[9] = {s, 0.f, 0.f, 0.f, s, 0.f, 0.f, 0.f, s};
+                const double s = k * prm[a] * prm[b];
+                const double H[9] = {s, 0.0, 0.0, 0.0, s, 0.0, 0.0, 0.0, s};
                 atomic_block(T.val, eb[a * S + b], H);
             }
         }
@@ -95,10 +104,10 @@ __device__ void assemble_element(const ImplicitTables &T, const float4 *__restri
     for (int a = 0; a < S; ++a)
 #pragma unroll
         for (int b = a + 1; b < S; ++b) {
-            V3A<float, 6> q[S];
-            seed_positions<float, S, 6>(p, a, q, b);
-            const VAD<float, 6> E = energy_ad(type, q, prm);
-            float Hab[9], Hba[9];
+            V3A<double, 6> q[S];
+            seed_positions<double, S, 6>(p, a, q, b);
+            const VAD<double, 6> E = energy_ad(type, q, prm);
+            double Hab[9], Hba[9];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -111,7 +120,7 @@ __device__ void assemble_element(const ImplicitTables &T, const float4 *__restri
             const bool diag_a = b == a + 1;
             const bool diag_b = a == S - 2 && b == S - 1;
             if (diag_a) {
-                float H[9];
+                double H[9];
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -120,7 +129,7 @@ __device__ void assemble_element(const ImplicitTables &T, const float4 *__restri
                 atomic_force(force, iv[a], E.g[0], E.g[1], E.g[2]);
             }
             if (diag_b) {
-                float H[9];
+                double H[9];
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -133,13 +142,13 @@ __device__ void assemble_element(const ImplicitTables &T, const float4 *__restri
 }
 
 __global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T, const float4 *__restrict__ pos,
-                                                                float4 *force, int n_elem)
+                                                                double *force, int n_elem)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_elem) return;
     const int4 ix = __ldg(T.idx + e);
     const int4 info = __ldg(T.info + e);
-    const float *prm = T.prm + info.y;
+    const double *prm = T.prm + info.y;
     switch (info.z) {
     case 1: {
         const int v = ix.x;
@@ -149,10 +158,10 @@ __global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T
         }
         // Anchor: 1/2 k |x - a|^2 on the anchor-relative position.
         const float4 b = pos[2 * v], d = pos[2 * v + 1];
-        const float xa[3] = {(b.x - prm[0]) + d.x, (b.y - prm[1]) + d.y, (b.z - prm[2]) + d.z};
-        const float k = prm[3];
+        const double xa[3] = {(double(b.x) - prm[0]) + d.x, (double(b.y) - prm[1]) + d.y, (double(b.z) - prm[2]) + d.z};
+        const double k = prm[3];
         atomic_force(force, v, k * xa[0], k * xa[1], k * xa[2]);
-        const float H[9] = {k, 0.f, 0.f, 0.f, k, 0.f, 0.f, 0.f, k};
+        const double H[9] = {k, 0.0, 0.0, 0.0, k, 0.0, 0.0, 0.0, k};
         atomic_block(T.val, T.eblk[size_t(e) * 16], H);
         return;
     }
@@ -164,8 +173,8 @@ __global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T
 
 // x0 = x (rebased: base = fl(x), dold = the exact remainder), y = x + h v as the delta, and the
 // forces initialised to M g.
-__global__ void implicit_predict_kernel(float4 *pos, float4 *dold, const float4 *vel, const float *mass, float4 *force,
-                                       int nv, float h, float gx, float gy, float gz)
+__global__ void implicit_predict_kernel(float4 *pos, float4 *dold, const float4 *vel, const float *mass, double *force,
+                                       int nv, float h, double gx, double gy, double gz)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
@@ -182,23 +191,26 @@ __global__ void implicit_predict_kernel(float4 *pos, float4 *dold, const float4 
     pos[2 * i] = make_float4(s[0], s[1], s[2], b.w);
     pos[2 * i + 1] = make_float4(r[0] + h * v.x, r[1] + h * v.y, r[2] + h * v.z, 0.f);
     dold[i] = make_float4(r[0], r[1], r[2], 0.f);
-    const float m = mass[i];
-    force[i] = make_float4(m * gx, m * gy, m * gz, 0.f);
+    const double m = mass[i];
+    force[3 * i] = m * gx;
+    force[3 * i + 1] = m * gy;
+    force[3 * i + 2] = m * gz;
 }
 
 // The mass term M / h^2 on the diagonal blocks and the diagonal preconditioner 1 / A_ii.
-__global__ void implicit_mass_kernel(ImplicitTables T, const float *mass, int nv, float invh2, float4 *dinv)
+__global__ void implicit_mass_kernel(ImplicitTables T, const float *mass, int nv, double invh2, double *dinv)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
-    float *b = T.val + size_t(T.diag[i]) * 9;
-    const float m = mass[i] * invh2;
+    double *b = T.val + size_t(T.diag[i]) * 9;
+    const double m = double(mass[i]) * invh2;
     b[0] += m;
     b[4] += m;
     b[8] += m;
     // Eigen's DiagonalPreconditioner: 1 / A_ii, or 1 where A_ii is 0.
-    dinv[i] = make_float4(b[0] != 0.f ? 1.f / b[0] : 1.f, b[4] != 0.f ? 1.f / b[4] : 1.f,
-                          b[8] != 0.f ? 1.f / b[8] : 1.f, 0.f);
+    dinv[3 * i] = b[0] != 0.0 ? 1.0 / b[0] : 1.0;
+    dinv[3 * i + 1] = b[4] != 0.0 ? 1.0 / b[4] : 1.0;
+    dinv[3 * i + 2] = b[8] != 0.0 ? 1.0 / b[8] : 1.0;
 }
 
 __device__ __forceinline__ void block_reduce_add(double v, double *out)
@@ -216,93 +228,84 @@ __device__ __forceinline__ void block_reduce_add(double v, double *out)
 }
 
 // Ap = A p (one thread per block row) and dots[0] += p . Ap.
-__global__ void implicit_spmv_kernel(ImplicitTables T, const float4 *__restrict__ p, float4 *Ap, int nv, double *dots)
+__global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double pap = 0.0;
     if (i < nv) {
-        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+        double y0 = 0.0, y1 = 0.0, y2 = 0.0;
         for (int k = __ldg(T.row_ptr + i); k < __ldg(T.row_ptr + i + 1); ++k) {
-            const float *b = T.val + size_t(k) * 9;
-            const float4 x = p[__ldg(T.col + k)];
-            y0 += b[0] * x.x + b[1] * x.y + b[2] * x.z;
-            y1 += b[3] * x.x + b[4] * x.y + b[5] * x.z;
-            y2 += b[6] * x.x + b[7] * x.y + b[8] * x.z;
+            const double *bl = T.val + size_t(k) * 9;
+            const double *x = p + 3 * size_t(__ldg(T.col + k));
+            y0 += bl[0] * x[0] + bl[1] * x[1] + bl[2] * x[2];
+            y1 += bl[3] * x[0] + bl[4] * x[1] + bl[5] * x[2];
+            y2 += bl[6] * x[0] + bl[7] * x[1] + bl[8] * x[2];
         }
-        Ap[i] = make_float4(y0, y1, y2, 0.f);
-        const float4 pi = p[i];
-        pap = double(pi.x) * y0 + double(pi.y) * y1 + double(pi.z) * y2;
+        Ap[3 * i] = y0;
+        Ap[3 * i + 1] = y1;
+        Ap[3 * i + 2] = y2;
+        pap = p[3 * i] * y0 + p[3 * i + 1] * y1 + p[3 * i + 2] * y2;
     }
     block_reduce_add(pap, dots);
 }
 
-// CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z.
-__global__ void implicit_cg_init_kernel(const float4 *b, const float4 *dinv, float4 *x, float4 *r, float4 *z,
-                                       float4 *p, int nv, double *dots)
+// CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z (per component).
+__global__ void implicit_cg_init_kernel(const double *b, const double *dinv, double *x, double *r, double *z,
+                                       double *p, int n, double *dots)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0, rz = 0.0;
-    if (i < nv) {
-        const float4 ri = b[i], di = dinv[i];
-        const float4 zi = make_float4(ri.x * di.x, ri.y * di.y, ri.z * di.z, 0.f);
-        x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        r[i] = make_float4(ri.x, ri.y, ri.z, 0.f);
+    if (i < n) {
+        const double ri = b[i], zi = ri * dinv[i];
+        x[i] = 0.0;
+        r[i] = ri;
         z[i] = zi;
         p[i] = zi;
-        rr = double(ri.x) * ri.x + double(ri.y) * ri.y + double(ri.z) * ri.z;
-        rz = double(ri.x) * zi.x + double(ri.y) * zi.y + double(ri.z) * zi.z;
+        rr = ri * ri;
+        rz = ri * zi;
     }
     block_reduce_add(rr, dots + 1);
     block_reduce_add(rz, dots + 2);
 }
 
 // x += alpha p; r -= alpha Ap; z = D^-1 r; dots[1] += r.r, dots[2] += r.z (alpha = rz / pAp).
-__global__ void implicit_cg_update_kernel(float4 *x, float4 *r, float4 *z, const float4 *p, const float4 *Ap,
-                                         const float4 *dinv, int nv, const double *prev, double *dots)
+__global__ void implicit_cg_update_kernel(double *x, double *r, double *z, const double *p, const double *Ap,
+                                         const double *dinv, int n, const double *prev, double *dots)
 {
-    const float alpha = static_cast<float>(prev[2] / prev[0]);
+    const double alpha = prev[2] / prev[0];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0, rz = 0.0;
-    if (i < nv) {
-        const float4 pi = p[i], api = Ap[i], di = dinv[i];
-        float4 xi = x[i], ri = r[i];
-        xi.x += alpha * pi.x;
-        xi.y += alpha * pi.y;
-        xi.z += alpha * pi.z;
-        ri.x -= alpha * api.x;
-        ri.y -= alpha * api.y;
-        ri.z -= alpha * api.z;
-        x[i] = xi;
+    if (i < n) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] - alpha * Ap[i];
         r[i] = ri;
-        const float4 zi = make_float4(ri.x * di.x, ri.y * di.y, ri.z * di.z, 0.f);
+        const double zi = ri * dinv[i];
         z[i] = zi;
-        rr = double(ri.x) * ri.x + double(ri.y) * ri.y + double(ri.z) * ri.z;
-        rz = double(ri.x) * zi.x + double(ri.y) * zi.y + double(ri.z) * zi.z;
+        rr = ri * ri;
+        rz = ri * zi;
     }
     block_reduce_add(rr, dots + 1);
     block_reduce_add(rz, dots + 2);
 }
 
 // p = z + beta p, beta = rz_new / rz_old.
-__global__ void implicit_cg_direction_kernel(float4 *p, const float4 *z, int nv, const double *prev, const double *cur)
+__global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, const double *prev, const double *cur)
 {
-    const float beta = static_cast<float>(cur[2] / prev[2]);
+    const double beta = cur[2] / prev[2];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nv) return;
-    const float4 zi = z[i], pi = p[i];
-    p[i] = make_float4(zi.x + beta * pi.x, zi.y + beta * pi.y, zi.z + beta * pi.z, 0.f);
+    if (i >= n) return;
+    p[i] = z[i] + beta * p[i];
 }
 
 // x = y + dx (the delta holds y).
-__global__ void implicit_apply_kernel(float4 *pos, const float4 *dx, int nv)
+__global__ void implicit_apply_kernel(float4 *pos, const double *dx, int nv)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     float4 d = pos[2 * i + 1];
-    const float4 a = dx[i];
-    d.x += a.x;
-    d.y += a.y;
-    d.z += a.z;
+    d.x = static_cast<float>(d.x + dx[3 * i]);
+    d.y = static_cast<float>(d.y + dx[3 * i + 1]);
+    d.z = static_cast<float>(d.z + dx[3 * i + 2]);
     pos[2 * i + 1] = d;
 }
 
@@ -359,7 +362,7 @@ struct ImplicitSolver {
         // Element list over every energy (internal vertex ids) and the block pattern.
         const int nv = L.nv;
         std::vector<I4> idx, info;
-        std::vector<float> prm;
+        std::vector<double> prm;
         std::vector<std::vector<int32_t>> nb(nv);
         for (int v = 0; v < nv; ++v) nb[v].push_back(v);
         for (int o = 0; o < scene->n_objects; ++o) {
@@ -373,7 +376,7 @@ struct ImplicitSolver {
                     for (int k = 0; k < S; ++k) iv[k] = L.ext2int[vb + E.stencils[int64_t(s) * S + k]];
                     idx.push_back({iv[0], iv[1], iv[2], iv[3]});
                     info.push_back({E.type, static_cast<int32_t>(prm.size()), S, 0});
-                    for (int k = 0; k < Pc; ++k) prm.push_back(static_cast<float>(E.params[int64_t(s) * Pc + k]));
+                    for (int k = 0; k < Pc; ++k) prm.push_back(E.params[int64_t(s) * Pc + k]);
                     for (int a = 0; a < S; ++a)
                         for (int b = 0; b < S; ++b)
                             if (a != b) nb[iv[a]].push_back(iv[b]);
@@ -407,7 +410,7 @@ struct ImplicitSolver {
             idx.push_back({0, -1, -1, -1});
             info.push_back({0, 0, 0, 0});
         }
-        if (prm.empty()) prm.push_back(0.f);
+        if (prm.empty()) prm.push_back(0.0);
         if (col.empty()) col.push_back(0);
         SPGX_TRY_STATUS(d_idx.upload(idx));
         SPGX_TRY_STATUS(d_info.upload(info));
@@ -417,13 +420,13 @@ struct ImplicitSolver {
         SPGX_TRY_STATUS(d_col.upload(col));
         SPGX_TRY_STATUS(d_diag.upload(diag.empty() ? std::vector<int32_t>{0} : diag));
         SPGX_TRY_STATUS(d_mass.upload(L.mass.empty() ? std::vector<float>{0.f} : L.mass));
-        SPGX_TRY_STATUS(d_val.alloc(size_t(std::max(1, nnzb)) * 9 * sizeof(float)));
-        const size_t vec = size_t(std::max(1, nv)) * sizeof(float4);
+        SPGX_TRY_STATUS(d_val.alloc(size_t(std::max(1, nnzb)) * 9 * sizeof(double)));
+        const size_t vec = size_t(std::max(1, nv)) * 3 * sizeof(double);
         for (DevBuf *b : {&d_force, &d_dinv, &d_x, &d_r, &d_z, &d_p, &d_Ap}) SPGX_TRY_STATUS(b->alloc(vec));
         SPGX_TRY_STATUS(d_dots.alloc(size_t(2) * 3 * sizeof(double)));
         SPGX_TRY_STATUS(h_dots.alloc(size_t(2) * 3 * sizeof(double)));
-        T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<float>(), d_eblk.as<int>(), d_row.as<int>(),
-                           d_col.as<int>(), d_val.as<float>(), d_diag.as<int>()};
+        T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
+                           d_col.as<int>(), d_val.as<double>(), d_diag.as<int>()};
         return SPGX_OK;
     }
 
@@ -435,9 +438,10 @@ struct ImplicitSolver {
         double *dots = d_dots.as<double>();  // two sets of {pAp, rr, rz}: [0..2] previous, [3..5] current
         double *hd = h_dots.as<double>();
         SPGX_CUDA(cudaMemsetAsync(dots, 0, 6 * sizeof(double), stream));
-        implicit_cg_init_kernel<<<grid_of(nv), 256, 0, stream>>>(d_force.as<float4>(), d_dinv.as<float4>(),
-                                                                 d_x.as<float4>(), d_r.as<float4>(), d_z.as<float4>(),
-                                                                 d_p.as<float4>(), nv, dots);
+        const int n = 3 * nv;
+        implicit_cg_init_kernel<<<grid_of(n), 256, 0, stream>>>(d_force.as<double>(), d_dinv.as<double>(),
+                                                                d_x.as<double>(), d_r.as<double>(), d_z.as<double>(),
+                                                                d_p.as<double>(), n, dots);
         SPGX_CUDA(cudaMemcpyAsync(hd, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
         SPGX_CUDA(cudaStreamSynchronize(stream));
         const double rhs2 = hd[1];
@@ -450,14 +454,14 @@ struct ImplicitSolver {
         while (rr >= thr2 && iterations < P.cg_max_iterations) {
             // prev = {pAp, rr, rz} of this iteration's start
             SPGX_CUDA(cudaMemsetAsync(prev, 0, sizeof(double), stream));
-            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, d_p.as<float4>(), d_Ap.as<float4>(), nv, prev);
+            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, d_p.as<double>(), d_Ap.as<double>(), nv, prev);
             SPGX_CUDA(cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream));
-            implicit_cg_update_kernel<<<grid_of(nv), 256, 0, stream>>>(d_x.as<float4>(), d_r.as<float4>(),
-                                                                      d_z.as<float4>(), d_p.as<float4>(),
-                                                                      d_Ap.as<float4>(), d_dinv.as<float4>(), nv,
-                                                                      prev, cur);
-            implicit_cg_direction_kernel<<<grid_of(nv), 256, 0, stream>>>(d_p.as<float4>(), d_z.as<float4>(), nv,
-                                                                          prev, cur);
+            implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(d_x.as<double>(), d_r.as<double>(),
+                                                                     d_z.as<double>(), d_p.as<double>(),
+                                                                     d_Ap.as<double>(), d_dinv.as<double>(), n, prev,
+                                                                     cur);
+            implicit_cg_direction_kernel<<<grid_of(n), 256, 0, stream>>>(d_p.as<double>(), d_z.as<double>(), n, prev,
+                                                                         cur);
             SPGX_CUDA(cudaMemcpyAsync(hd, cur, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
             SPGX_CUDA(cudaStreamSynchronize(stream));
             rr = hd[1];
@@ -479,15 +483,14 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaEventRecord(ev0, stream));
         for (int s = 0; s < P.substeps && nv > 0; ++s) {
             implicit_predict_kernel<<<grid_of(nv), 256, 0, stream>>>(X.pos(), X.dold(), X.vel(), d_mass.as<float>(),
-                                                                     d_force.as<float4>(), nv, float(h),
-                                                                     float(P.gravity[0]), float(P.gravity[1]),
-                                                                     float(P.gravity[2]));
-            SPGX_CUDA(cudaMemsetAsync(d_val.as<float>(), 0, size_t(std::max(1, nnzb)) * 9 * sizeof(float), stream));
+                                                                     d_force.as<double>(), nv, float(h), P.gravity[0],
+                                                                     P.gravity[1], P.gravity[2]);
+            SPGX_CUDA(cudaMemsetAsync(d_val.as<double>(), 0, size_t(std::max(1, nnzb)) * 9 * sizeof(double), stream));
             if (n_elem > 0)
-                implicit_assemble_kernel<<<grid_of(n_elem, 128), 128, 0, stream>>>(T, X.pos(), d_force.as<float4>(),
+                implicit_assemble_kernel<<<grid_of(n_elem, 128), 128, 0, stream>>>(T, X.pos(), d_force.as<double>(),
                                                                                   n_elem);
-            implicit_mass_kernel<<<grid_of(nv), 256, 0, stream>>>(T, d_mass.as<float>(), nv, float(1.0 / (h * h)),
-                                                                  d_dinv.as<float4>());
+            implicit_mass_kernel<<<grid_of(nv), 256, 0, stream>>>(T, d_mass.as<float>(), nv, 1.0 / (h * h),
+                                                                  d_dinv.as<double>());
             SPGX_CUDA(cudaGetLastError());
             int its = 0;
             double rel = 0.0;
@@ -495,7 +498,7 @@ struct ImplicitSolver {
             st.iterations += its;
             st.residual_final = rel;
             if (rel > P.cg_threshold) st.converged = 0;
-            implicit_apply_kernel<<<grid_of(nv), 256, 0, stream>>>(X.pos(), d_x.as<float4>(), nv);
+            implicit_apply_kernel<<<grid_of(nv), 256, 0, stream>>>(X.pos(), d_x.as<double>(), nv);
             launch_end_substep(X, h, stream);
         }
         SPGX_CUDA(cudaEventRecord(ev1, stream));
