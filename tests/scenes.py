@@ -180,3 +180,22 @@ def spring_variant(n=9, load=False):
         weight = float(s.mass.max()) * 9.81
         energies.append(_energy(O.STATIC_LOAD, bottom, np.tile(np.concatenate([[weight], d]), (n, 1))))
     return O.SceneObject(s.x.copy(), s.mass.copy(), energies, None, s.x0.copy())
+
+
+def truss_variant(nx=5, ny=3, nz=3, k_cont=2e3, k_sq=5e2):
+    """The SNH bar's tet edges as continuum springs (12) and squared continuum springs (13),
+    with its anchors: a 3D truss, well conditioned for implicit solves (a flat cloth at rest has
+    no transverse stiffness)."""
+    b = beam_cfg2(nx, ny, nz)
+    tets = next(e for e in b.energies if e.type == O.SNH).stencils
+    pairs = set()
+    for t in tets:
+        for i in range(4):
+            for j in range(i + 1, 4):
+                pairs.add((min(t[i], t[j]), max(t[i], t[j])))
+    pairs = np.array(sorted(pairs), dtype=np.int32)
+    energies = [_energy(O.SPRING_CONT, pairs, continuum_spring_params(b.x0, pairs, k_cont)),
+                _energy(O.SPRING_SQ_CONT, pairs, continuum_spring_params(b.x0, pairs, k_sq))]
+    energies += [e for e in b.energies if e.type == O.ANCHOR]
+    return O.SceneObject(b.x.copy(), b.mass.copy(), energies, None, b.x0.copy())
+

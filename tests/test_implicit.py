@@ -1,6 +1,8 @@
 """Implicit Euler (one Newton step per substep, the reference's ImplicitEulerNewtonDx): the
 FP64 oracle's conjugate-gradient restatement against a direct solve (CPU), and the GPU
-solver against the oracle on scenes with every energy type (GB300)."""
+solver against the oracle on scenes with every energy type (GB300). Continuum springs run on
+a 3D truss: on a flat cloth at rest the implicit step is nearly singular out of plane, and a
+1e-9 m perturbation grows to millimetres in one step in the FP64 oracle itself."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -19,7 +21,7 @@ def _scenes():
         "stvk_tet_load": scenes.beam_tet_variant(O.STVK_TET, nx=5, ny=3, nz=3, load=True),
         "bw": scenes.cloth_variant((O.BW_MEMBRANE, O.BW_BENDING), rows=7),
         "choi_quad": scenes.cloth_variant((O.CHOI_MEMBRANE, O.QUAD_BENDING), rows=7),
-        "springs": scenes.spring_variant(n=7),
+        "truss": scenes.truss_variant(),
     }
 
 
@@ -45,7 +47,7 @@ def test_oracle_steps_every_scene():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["stvk_cloth", "snh_beam", "spring_cloth", "stvk_tet_load", "bw", "choi_quad",
-                                  "springs"])
+                                  "truss"])
 def test_positions_after_10_steps_match_oracle(name):
     N = pytest.importorskip("spg_gb300.native")
     obj = _scenes()[name]
