@@ -273,7 +273,20 @@ def other_configs(local) -> dict:
                                      "vertices": nv, "colors": int(s.n_colors(-1)), "launch": list(s.launch()),
                                      "graph": True}
     s.close()
+    imp = N.ImplicitSolver([cloth], dt=1 / 60, substeps=1, gravity=GRAVITY, device=local)
+    stats = [imp.step() for _ in range(8)][3:]
+    out["implicit_euler_cloth_33x33"] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
+                                         "cg_iterations": [int(st.iterations) for st in stats],
+                                         "precision": "FP64 assembly and CG"}
+    imp.close()
     big = S.spring_cloth(ROWS).objects[0]
+    imp = N.ImplicitSolver([big], dt=DT, substeps=1, gravity=GRAVITY, device=local)
+    stats = [imp.step() for _ in range(4)][1:]
+    out["implicit_euler_spring_cloth_513"] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
+                                              "cg_iterations": [int(st.iterations) for st in stats],
+                                              "converged": [bool(st.converged) for st in stats],
+                                              "precision": "FP64 assembly and CG"}
+    imp.close()
     x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local)
     ms = statistics.mean(_timed_steps(x, 5))
     out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
