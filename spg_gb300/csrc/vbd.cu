@@ -155,21 +155,50 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
                                                                 int epoch_base, int max_local, float invdt2,
                                                                 float fb2)
 {
+    // Shared memory: base and delta positions of the local vertices, the record block, and the
+    // global indices of the next task's local vertices (fetched while the current one runs).
     extern __shared__ float4 dyn[];
     float4 *sb = dyn;
     float4 *sd = dyn + max_local;
     int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
-    __shared__ int s_task, s_fail;
+    __shared__ int s_next, s_fail;
     const int total = iterations * n_tiles;
     const int lv = threadIdx.x / G;
     const int lane = threadIdx.x & (G - 1);
-    for (;;) {
-        if (threadIdx.x == 0) s_task = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
-        __syncthreads();
-        const int task = s_task;
-        if (task >= total) break;
+    int *sidx = reinterpret_cast<int *>(srec + V.max_records);
+
+    // Static data of a task: its header, the indices of its local vertices (into sidx, async)
+    // and the header and record offset of the thread's vertex.
+    auto fetch_static = [&](int task, int4 &h0, int4 &h1, int4 &hv, int &roff) {
+        const int tile = task % n_tiles;
+        h0 = __ldg(V.hdr + 2 * tile);
+        h1 = __ldg(V.hdr + 2 * tile + 1);
+        const int nvt = h0.y, nl = h0.y + h0.w;
+        for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+            if (i < nvt)
+                sidx[i] = h0.x + i;
+            else
+                cp_async4(sidx + i, V.halo + h0.z + i - nvt);
+        }
+        hv = make_int4(0, 0, 0, 0);
+        roff = 0;
+        if (lv < nvt) {
+            hv = __ldg(S.hdr + h0.x + lv);
+            roff = __ldg(V.vrec + h0.x + lv);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    if (threadIdx.x == 0) s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
+    __syncthreads();
+    int task = s_next;
+    int4 h0, h1, hv;
+    int roff;
+    if (task < total) fetch_static(task, h0, h1, hv, roff);
+    while (task < total) {
         const int k = task / n_tiles;
         const int tile = task - k * n_tiles;
+        // Wait for the tiles this sweep reads (warp 0 polls, one neighbour per lane).
         if (threadIdx.x < 32) {
             const int c = __ldg(F.tile_color + tile);
             const int b = __ldg(F.nbr_off + tile), e = __ldg(F.nbr_off + tile + 1);
@@ -189,7 +218,8 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             ok = __all_sync(0xffffffffu, ok);
             if (threadIdx.x == 0) s_fail = !ok;
         }
-        __syncthreads();
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // this thread's index copies
+        __syncthreads();  // every thread's index copies, and the poll result
         if (s_fail) {
             if (threadIdx.x == 0) {
                 atomicExch(F.ticket + 1, 1);
@@ -197,9 +227,20 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             }
             break;
         }
-        TileVertex tv;
-        const int4 h0 = tile_stage<G>(V, S, tile, sb, sd, srec, tv);
+        // Stage the records and the current positions of the local vertices.
+        for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
+        const int nl = h0.y + h0.w;
+        for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+            const int g = sidx[i];
+            cp_async16(sb + i, S.pos + 2 * g);
+            cp_async16(sd + i, S.pos + 2 * g + 1);
+        }
         const bool active = lv < h0.y;
+        float4 tg = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (active) tg = S.tgt[h0.x + lv];
+        if (threadIdx.x == 0) s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
+        cp_async_wait_all();
+        __syncthreads();
         TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
         if (active) {
             cx.bs = v3(sb[lv]);
@@ -207,14 +248,16 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         }
         Block<float> acc;
         block_zero(acc);
-        tile_vertex_accumulate<G>(cx, tv.hv, tv.roff, lane, acc);
+        tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
         group_reduce<G>(acc);
-        if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tv.tg, invdt2, fb2);
-        __syncthreads();  // every position of the tile is written (and the staging is consumed)
+        if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tg, invdt2, fb2);
+        __syncthreads();  // every position of the tile is written, the staging consumed, s_next set
         if (threadIdx.x == 0) {
             __threadfence();
             st_release_gpu(F.epoch + tile, epoch_base + k + 1);
         }
+        task = s_next;
+        if (task < total) fetch_static(task, h0, h1, hv, roff);
     }
 }
 
@@ -584,6 +627,7 @@ spgx_status VbdSolver::setup_tiles()
     TV.halo = tb_halo.as<int>();
     TV.records = tb_records.as<int4>();
     TV.vrec = tb_vrec.as<int>();
+    TV.max_records = std::max(1, TL.max_records);
     tile_smem = tile_smem_bytes(std::max(1, TL.max_local), std::max(1, TL.max_records));
     // The opt-in limit is declared once for every tile kernel, whatever this scene needs: the
     // attribute is process-wide, so a per-scene value would break a larger scene's live

@@ -22,6 +22,7 @@ struct TileView {
     const int *halo;
     const int4 *records;
     const int *vrec;      // per internal vertex: record offset inside its tile's block
+    int max_records;      // 16-byte record units of the largest tile
 };
 
 // Tables of the dataflow kernel (vbd_flow_kernel).
@@ -33,15 +34,23 @@ struct FlowView {
     int *ticket;            // [0] next task, [1] abort flag (both zeroed before a launch)
 };
 
+// Positions (base + delta) of the local vertices and the record block; the dataflow kernel
+// also keeps the next task's local-vertex indices (4 B each).
 inline size_t tile_smem_bytes(int max_local, int max_records)
 {
-    return size_t(2 * max_local) * 16 + size_t(max_records) * 16;
+    return size_t(2 * max_local) * 16 + size_t(max_records) * 16 + size_t(max_local) * 4;
 }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
 __device__ __forceinline__ void cp_async_wait_all()
