@@ -338,7 +338,8 @@ def run_gb300(args, dist, rank, local, ws):
     scene = S.spring_cloth(ROWS)
     obj = scene.objects[0]
     solver = N.VbdSolver([obj], dt=DT, iterations=ITERATIONS, gravity=GRAVITY, device=local,
-                         lanes_per_vertex=args.lanes, block_size=args.block, kernel=args.kernel)
+                         lanes_per_vertex=args.lanes, block_size=args.block, kernel=args.kernel,
+                         tile_vertices=args.tile)
     kernel, lanes, block = solver.launch()
     nv = obj.nv
 
@@ -408,7 +409,7 @@ def run_gb300(args, dist, rank, local, ws):
                    "kernel": {1: "lanes-per-vertex", 2: "shared-memory tiles, one launch per colour",
                               3: "shared-memory tiles, dataflow (one persistent launch per step)"}[kernel],
                    "lanes_per_vertex": lanes, "block_size": block,
-                   "tile_vertices": (solver.params.tile_vertices or 64) if kernel >= 2 else None,
+                   "tile_vertices": block // lanes if kernel >= 2 else None,
                    "colors": int(solver.n_colors(-1)),
                    "parallelism": "replicas" if ws > 1 else "single GPU", "wall_s_timed_region": wall},
         "gpu_launches": launches_per_step * args.steps,
@@ -442,6 +443,7 @@ def main():
     ap.add_argument("--skip-extras", action="store_true", help="skip time-to-residual and the other configs")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0 = autotune)")
+    ap.add_argument("--tile", type=int, default=0, help="vertices per tile of kernels 2 and 3 (0 = autotune)")
     ap.add_argument("--kernel", type=int, default=0,
                     help="1 = lanes per vertex, 2 = tiles, 3 = dataflow tiles (0 = autotune)")
     args = ap.parse_args()

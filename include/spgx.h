@@ -155,12 +155,13 @@ typedef struct spgx_vbd_params {
                                 * (one launch per colour), 3 = dataflow tile kernel (one persistent
                                 * cooperative launch runs all sweeps; a tile starts as soon as its
                                 * neighbour tiles finished the sweeps it reads; no CUDA graph needed) */
-    int32_t tile_vertices;     /* vertices per tile of the tile kernels (1..128; 0 = 64) */
+    int32_t tile_vertices;     /* vertices per tile of the tile kernels (1..128; 0 = autotune over 32
+                                * and 64); the chosen size is block_size / lanes_per_vertex */
 } spgx_vbd_params;
 
 /* Defaults: dt 0.01, 1 substep, 1 iteration, gravity (0,-9.8,0) (baseSolver.h:36-38),
  * tolerance 0, max_iterations 1000, check_interval 10, fallback_condition 1e6, autotune,
- * use_graph 1, device 0, kernel autotune, 64 vertices per tile. */
+ * use_graph 1, device 0, kernel and tile size autotuned. */
 void spgx_vbd_params_default(spgx_vbd_params *p);
 
 typedef struct spgx_step_stats {

@@ -61,7 +61,7 @@ void spgx_vbd_params_default(spgx_vbd_params *p)
     p->use_graph = 1;
     p->device = 0;
     p->kernel = 0;
-    p->tile_vertices = 64;
+    p->tile_vertices = 0;
 }
 
 void spgx_xpbd_params_default(spgx_xpbd_params *p)

@@ -604,16 +604,15 @@ spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params 
     S.adj = d_adj.as<int>();
     S.counters = d_counters.as<int>();
     S.status = reinterpret_cast<unsigned int *>(d_counters.as<int>() + 2);
-    SPGX_TRY_STATUS(setup_tiles());
+    SPGX_TRY_STATUS(setup_tiles(P.tile_vertices ? P.tile_vertices : kTileCandidates[0]));
     SPGX_TRY_STATUS(setup_flow());
     SPGX_TRY_STATUS(configure_launch());
     return SPGX_OK;
 }
 
-spgx_status VbdSolver::setup_tiles()
+spgx_status VbdSolver::setup_tiles(int tv)
 {
     std::string err;
-    const int tv = P.tile_vertices ? P.tile_vertices : 64;
     const spgx_status st = build_tiles(L, tv, TL, err);
     if (st != SPGX_OK) {
         set_error(err);
@@ -771,16 +770,17 @@ spgx_status VbdSolver::set_params(const spgx_vbd_params *params)
 }
 
 // Picks the kernel and its launch shape. Explicit parameters win; otherwise every candidate
-// (the lanes kernel with lanes up to twice the mean vertex degree and blocks 64/128/256, and
-// the tile kernel with 64/128/256 threads) is timed on two colour sweeps of this scene and the
-// fastest kept. The positions are restored afterwards.
+// is timed on two sweeps of this scene and the fastest kept: the lanes kernel with lanes up to
+// twice the mean vertex degree and blocks of 64/128/256 threads, and the tile and dataflow
+// kernels with 1/2/4/8 lanes per vertex on tiles of each size in kTileCandidates (or the
+// requested size). The scene is re-tiled for each tile size tried and left tiled for the pick;
+// the positions are restored afterwards.
 spgx_status VbdSolver::configure_launch()
 {
     graph_valid = false;
     struct Cand {
-        int kernel, lanes, block;
+        int kernel, lanes, block, tile;
     };
-    std::vector<Cand> cands;
     const bool want_lanes = P.kernel == 0 || P.kernel == 1;
     // Energies of types 6-14 are evaluated by the lanes kernel only (they are not in the
     // tile records).
@@ -791,12 +791,37 @@ spgx_status VbdSolver::configure_launch()
     }
     const bool want_tiles = !generic && (P.kernel == 0 || P.kernel == 2);
     const bool want_flow = !generic && (P.kernel == 0 || P.kernel == 3);
-    std::vector<int> blocks;
-    if (P.block_size)
-        blocks.push_back(P.block_size);
-    else
-        blocks = {64, 128, 256};
+    std::vector<int> tile_sizes;
+    if (P.tile_vertices)
+        tile_sizes.push_back(P.tile_vertices);
+    else if (want_tiles || want_flow)
+        tile_sizes.assign(std::begin(kTileCandidates), std::end(kTileCandidates));
+    // Candidates of one tile size; the flow candidates read the occupancy of the current tiling.
+    auto tile_cands = [&](int T, std::vector<Cand> &out) {
+        if (want_tiles)
+            for (int g : {1, 2, 4, 8})
+                if (T * g <= kTileThreads && (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
+                    out.push_back({2, g, T * g, T});
+        if (want_flow)
+            for (int g : {1, 2, 4, 8}) {
+                const int li = g == 1 ? 0 : g == 2 ? 1 : g == 4 ? 2 : 3;
+                if (T * g <= kTileThreads && T * g >= 32 && flow_blocks_per_sm[li] > 0 &&
+                    (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
+                    out.push_back({3, g, T * g, T});
+            }
+    };
+    auto retile = [&](int T) -> spgx_status {
+        if (TL.tile_vertices == T) return SPGX_OK;
+        SPGX_TRY_STATUS(setup_tiles(T));
+        return setup_flow();
+    };
+    std::vector<Cand> lane_cands;
     if (want_lanes) {
+        std::vector<int> blocks;
+        if (P.block_size)
+            blocks.push_back(P.block_size);
+        else
+            blocks = {64, 128, 256};
         std::vector<int> lane_opts;
         if (P.lanes_per_vertex)
             lane_opts.push_back(P.lanes_per_vertex);
@@ -804,63 +829,79 @@ spgx_status VbdSolver::configure_launch()
             for (int g : {1, 2, 4, 8, 16, 32})
                 if (g == 1 || g <= 2 * std::max(1.0, L.mean_degree)) lane_opts.push_back(g);
         for (int g : lane_opts)
-            for (int b : blocks) cands.push_back({1, g, b});
+            for (int b : blocks) lane_cands.push_back({1, g, b, 0});
     }
-    if (want_tiles)
-        for (int g : {1, 2, 4, 8})
-            if (TL.tile_vertices * g <= kTileThreads && (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
-                cands.push_back({2, g, TL.tile_vertices * g});
-    if (want_flow)
-        for (int g : {1, 2, 4, 8}) {
-            const int li = g == 1 ? 0 : g == 2 ? 1 : g == 4 ? 2 : 3;
-            if (TL.tile_vertices * g <= kTileThreads && TL.tile_vertices * g >= 32 && flow_blocks_per_sm[li] > 0 &&
-                (P.lanes_per_vertex == 0 || P.lanes_per_vertex == g))
-                cands.push_back({3, g, TL.tile_vertices * g});
+    // A single candidate (or an empty scene) needs no timing.
+    if (tile_sizes.size() <= 1) {
+        std::vector<Cand> all = lane_cands;
+        if (!tile_sizes.empty()) {
+            SPGX_TRY_STATUS(retile(tile_sizes[0]));
+            tile_cands(tile_sizes[0], all);
         }
-    if (cands.empty()) {
-        set_error("no kernel variant fits the requested launch parameters");
-        return SPGX_ERR_INVALID_ARG;
-    }
-    if (cands.size() == 1 || L.nv == 0) {
-        kernel = cands[0].kernel;
-        lanes = cands[0].lanes;
-        block = cands[0].block;
-        return SPGX_OK;
+        if (all.empty()) {
+            set_error("no kernel variant fits the requested launch parameters");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        if (all.size() == 1 || L.nv == 0) {
+            kernel = all[0].kernel;
+            lanes = all[0].lanes;
+            block = all[0].block;
+            return SPGX_OK;
+        }
     }
     SPGX_TRY_STATUS(X.upload_if_dirty(stream));
     SPGX_CUDA(cudaMemcpyAsync(d_backup.as<void>(), S.pos, size_t(L.nv) * 2 * sizeof(float4),
                               cudaMemcpyDeviceToDevice, stream));
     float best = 1e30f;
-    Cand pick = cands[0];
-    for (const auto &c : cands) {
-        kernel = c.kernel;
-        lanes = c.lanes;
-        block = c.block;
-        launch_iterations(*this, 1, stream);
-        SPGX_CUDA(cudaEventRecord(ev0, stream));
-        launch_iterations(*this, 2, stream);
-        SPGX_CUDA(cudaEventRecord(ev1, stream));
-        SPGX_CUDA(cudaEventSynchronize(ev1));
-        float ms = 0.f;
-        SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-        if (ms < best) {
-            best = ms;
-            pick = c;
+    Cand pick{};
+    bool have_pick = false;
+    auto time_all = [&](const std::vector<Cand> &cs) -> spgx_status {
+        for (const auto &c : cs) {
+            kernel = c.kernel;
+            lanes = c.lanes;
+            block = c.block;
+            launch_iterations(*this, 1, stream);
+            SPGX_CUDA(cudaEventRecord(ev0, stream));
+            launch_iterations(*this, 2, stream);
+            SPGX_CUDA(cudaEventRecord(ev1, stream));
+            SPGX_CUDA(cudaEventSynchronize(ev1));
+            float ms = 0.f;
+            SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            if (!have_pick || ms < best) {
+                best = ms;
+                pick = c;
+                have_pick = true;
+            }
+            SPGX_CUDA(cudaMemcpyAsync(S.pos, d_backup.as<void>(), size_t(L.nv) * 2 * sizeof(float4),
+                                      cudaMemcpyDeviceToDevice, stream));
         }
-        SPGX_CUDA(cudaMemcpyAsync(S.pos, d_backup.as<void>(), size_t(L.nv) * 2 * sizeof(float4),
-                                  cudaMemcpyDeviceToDevice, stream));
+        // A dataflow sweep that gave up leaves its tiles' epochs behind: check before the
+        // next tiling replaces them.
+        int *hc = h_counters.as<int>();
+        SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), kCounters * sizeof(int), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, kCounters * sizeof(int), stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        SPGX_CUDA(cudaGetLastError());
+        SPGX_TRY_STATUS(take_flow_launch_error());
+        if (hc[2] & 2u) {
+            SPGX_TRY_STATUS(reset_flow());
+            set_error("a dataflow sweep gave up waiting for a neighbour tile while timing launch shapes");
+            return SPGX_ERR_TIMEOUT;
+        }
+        return SPGX_OK;
+    };
+    SPGX_TRY_STATUS(time_all(lane_cands));
+    for (int T : tile_sizes) {
+        SPGX_TRY_STATUS(retile(T));
+        std::vector<Cand> tc;
+        tile_cands(T, tc);
+        SPGX_TRY_STATUS(time_all(tc));
     }
-    int *hc = h_counters.as<int>();
-    SPGX_CUDA(cudaMemcpyAsync(hc, d_counters.as<int>(), kCounters * sizeof(int), cudaMemcpyDeviceToHost, stream));
-    SPGX_CUDA(cudaMemsetAsync(d_counters.as<int>(), 0, kCounters * sizeof(int), stream));
-    SPGX_CUDA(cudaStreamSynchronize(stream));
-    SPGX_CUDA(cudaGetLastError());
-    SPGX_TRY_STATUS(take_flow_launch_error());
-    if (hc[2] & 2u) {
-        SPGX_TRY_STATUS(reset_flow());
-        set_error("a dataflow sweep gave up waiting for a neighbour tile while timing launch shapes");
-        return SPGX_ERR_TIMEOUT;
+    if (!have_pick) {
+        set_error("no kernel variant fits the requested launch parameters");
+        return SPGX_ERR_INVALID_ARG;
     }
+    if (pick.tile) SPGX_TRY_STATUS(retile(pick.tile));
     kernel = pick.kernel;
     lanes = pick.lanes;
     block = pick.block;

@@ -62,7 +62,7 @@ struct VbdSolver {
     static spgx_status check_params(const spgx_vbd_params *p);
     spgx_status set_params(const spgx_vbd_params *params);
     spgx_status configure_launch();
-    spgx_status setup_tiles();
+    spgx_status setup_tiles(int tile_vertices);
     spgx_status setup_flow();
     spgx_status reset_flow();
     spgx_status take_flow_launch_error();

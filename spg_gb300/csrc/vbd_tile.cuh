@@ -16,6 +16,9 @@
 namespace spgx {
 
 constexpr int kTileThreads = 256;  // maximum threads per tile CTA (tile vertices x lanes)
+// Tile sizes (vertices per tile) the launch autotuner tries when none is requested; the first
+// is the tiling a solver starts with.
+constexpr int kTileCandidates[2] = {32, 64};
 
 struct TileView {
     const int4 *hdr;      // 2 per tile

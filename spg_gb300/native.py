@@ -179,7 +179,7 @@ class Descriptor:
 
 def vbd_params(dt=0.01, substeps=1, iterations=1, gravity=(0.0, -9.8, 0.0), tolerance=0.0, max_iterations=1000,
                check_interval=10, fallback_condition=1e6, lanes_per_vertex=0, block_size=0, use_graph=1,
-               device=0, kernel=0, tile_vertices=64) -> VbdParams:
+               device=0, kernel=0, tile_vertices=0) -> VbdParams:
     p = VbdParams()
     lib().spgx_vbd_params_default(C.byref(p))
     p.dt, p.substeps, p.iterations = dt, substeps, iterations

@@ -36,7 +36,7 @@ def test_sizes_and_defaults():
         assert lib.spgx_param_count(t) == N.PARAM_COUNT[t]
     assert lib.spgx_stencil_size(42) == 0
     p = N.vbd_params()
-    assert p.fallback_condition == 1e6 and p.use_graph == 1 and p.tile_vertices == 64
+    assert p.fallback_condition == 1e6 and p.use_graph == 1 and p.tile_vertices == 0
 
 
 def _has_device():

@@ -164,17 +164,17 @@ def test_colors_and_adjacency_through_handle():
     assert np.array_equal(c1, c2) and np.array_equal(e1, e2)
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4])
-def test_dataflow_kernel_equals_colour_launches(lanes):
+@pytest.mark.parametrize("lanes,tile", [(1, 64), (2, 64), (4, 64), (4, 32), (2, 32)])
+def test_dataflow_kernel_equals_colour_launches(lanes, tile):
     """The dataflow kernel runs the same Gauss-Seidel order as one launch per colour, so with
     the same lanes per vertex (same per-vertex summation order) it gives the same positions
     bit for bit, over steps of 20 sweeps and for a tolerance-mode step."""
     from spg_gb300 import scenes as S
     obj = S.spring_cloth(129).objects[0]
-    kw = dict(dt=1 / 120, iterations=20, gravity=scenes.GRAVITY, lanes_per_vertex=lanes)
+    kw = dict(dt=1 / 120, iterations=20, gravity=scenes.GRAVITY, lanes_per_vertex=lanes, tile_vertices=tile)
     a = N.VbdSolver([obj], kernel=2, **kw)
     b = N.VbdSolver([obj], kernel=3, **kw)
-    assert a.launch() == (2, lanes, 64 * lanes) and b.launch() == (3, lanes, 64 * lanes)
+    assert a.launch() == (2, lanes, tile * lanes) and b.launch() == (3, lanes, tile * lanes)
     for _ in range(3):
         a.step()
         b.step()
@@ -184,3 +184,23 @@ def test_dataflow_kernel_equals_colour_launches(lanes):
     sa, sb = a.step(), b.step()
     assert sa.iterations == sb.iterations
     assert np.array_equal(a.state(0)[0], b.state(0)[0])
+
+
+@pytest.mark.parametrize("kernel", [0, 2, 3])
+def test_autotuned_tile_size(kernel):
+    """With no tile size requested the autotuner tries 32- and 64-vertex tiles and leaves the
+    scene tiled for its pick: the solver then steps exactly as one created with that size."""
+    from spg_gb300 import scenes as S
+    obj = S.spring_cloth(129).objects[0]
+    kw = dict(dt=1 / 120, iterations=20, gravity=scenes.GRAVITY)
+    a = N.VbdSolver([obj], kernel=kernel, **kw)
+    k, g, b = a.launch()
+    if k == 1:
+        pytest.skip("the lanes kernel won on this device")
+    assert k in (2, 3) and b // g in (32, 64) and b % g == 0
+    ref = N.VbdSolver([obj], kernel=k, lanes_per_vertex=g, tile_vertices=b // g, **kw)
+    assert ref.launch() == (k, g, b)
+    for _ in range(3):
+        a.step()
+        ref.step()
+    assert np.array_equal(a.state(0)[0], ref.state(0)[0])
