@@ -292,6 +292,52 @@ def other_configs(local) -> dict:
     out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
                                                "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3)}
     x.close()
+    out["mesh_input"] = mesh_input()
+    return out
+
+
+def mesh_input() -> dict:
+    """Host mesh readers (spg::io::loadObj / loadMsh) on files written from the benchmark
+    meshes: the 513x513 cloth as OBJ and an 81x21x21 six-tet bar as MSH 4.1 (ASCII and
+    binary). Median wall time of three reads each."""
+    import tempfile
+
+    from spg_gb300 import scenes as S
+    from tests import meshfiles as MF
+
+    def faces(n):
+        """The triangles of the grid builder (alternating diagonals), row by row."""
+        import numpy as np
+        r, c = (a.ravel() for a in np.meshgrid(np.arange(1, n), np.arange(1, n), indexing="ij"))
+        even = ((r + c) % 2 == 0)[:, None]
+        ll, ul, ur, lr = r * n + c - 1, (r - 1) * n + c - 1, (r - 1) * n + c, r * n + c
+        t1 = np.where(even, np.stack([ll, ul, ur], 1), np.stack([ul, lr, ll], 1))
+        t2 = np.where(even, np.stack([ll, ur, lr], 1), np.stack([ul, ur, lr], 1))
+        return np.stack([t1, t2], 1).reshape(-1, 3)
+
+    def timed(fn, path):
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            V, C = fn(path)
+            ts.append(time.perf_counter() - t0)
+        ms = 1e3 * statistics.median(ts)
+        return {"ms": ms, "mb_per_s": os.path.getsize(path) / 1e6 / (ms * 1e-3), "vertices": len(V), "cells": len(C),
+                "file_mb": os.path.getsize(path) / 1e6}
+
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        cloth = S.spring_cloth(ROWS).objects[0]
+        p = os.path.join(d, "cloth.obj")
+        MF.write_obj(p, cloth.x0, faces(ROWS))
+        out["obj_cloth_513"] = timed(S.load_obj, p)
+        bar = S.tet_beam(81, 21, 21).objects[0]
+        T = next(e for e in bar.energies if e.stencils.shape[1] == 4).stencils
+        for binary in (False, True):
+            q = os.path.join(d, f"bar_{int(binary)}.msh")
+            MF.write_msh41(q, bar.x0, T, binary=binary, node_blocks=4)
+            out["msh41_bar_81x21x21_" + ("binary" if binary else "ascii")] = timed(S.load_msh, q)
+    out["threads"] = 1
     return out
 
 

@@ -42,4 +42,19 @@ ParticleGroup createTetrahedralBeam(Real mass, float sideX, float sideY, float s
 std::vector<ParticleGroup> createPatchBatch(int nPatches, int nMin, int nMax, Real muLo, Real muHi, Real kbLo,
                                             Real kbHi, Real mass, Real anchorStiffness, uint64_t seed);
 
+// A shell on a loaded triangle mesh (spg::io::loadObj), assembled as createSpringCloth
+// assembles its grid: masses lumped from the rest areas, springs on every edge, discrete
+// bending on interior edges, anchors on the given vertices. Rest = initial = the mesh's
+// vertices, which may lie anywhere in 3D. Energy order: bending, spring, anchor.
+ParticleGroup createTriangleMeshShell(const std::vector<Vector3> &vertices, const std::vector<Int3> &faces, Real mass,
+                                      Real springStiffness, Real bendingStiffness, Real anchorStiffness,
+                                      const std::vector<int> &anchorIds);
+
+// A solid on a loaded tetrahedral mesh (spg::io::loadMsh), assembled as createTetrahedralBeam
+// assembles its bar: masses lumped from the rest volumes, Stable Neo-Hookean tets, anchors
+// on the given vertices. Tets must have positive rest volume (StableNeoHookeanEnergy throws
+// otherwise). Energy order: anchor, tet.
+ParticleGroup createTetMeshSolid(const std::vector<Vector3> &vertices, const std::vector<Int4> &tets, Real mass,
+                                 Real young, Real poisson, Real anchorStiffness, const std::vector<int> &anchorIds);
+
 }  // namespace spg::scenes

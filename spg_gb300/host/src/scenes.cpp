@@ -248,6 +248,51 @@ ParticleGroup createTetrahedralBeam(Real mass, float sx, float sy, float sz, int
     return pGroup;
 }
 
+ParticleGroup createTriangleMeshShell(const std::vector<Vector3> &vertices, const std::vector<Int3> &faces, Real mass,
+                                      Real springStiffness, Real bendingStiffness, Real anchorStiffness,
+                                      const std::vector<int> &anchorIds)
+{
+    const TriangleMesh mesh(vertices, vertices, faces);
+    ParticleGroup pGroup;
+    addClothParticles(pGroup, mesh, mass, true);
+    auto bending = clothBending(mesh, bendingStiffness);
+    pGroup.addEnergy(bending);
+    bending->preparePrecomputations(pGroup);
+    auto springs = std::make_shared<SpringEnergy>();
+    for (const auto &e : mesh.edges())
+        springs->addStencil({e[0], e[1]}, (pGroup.positions0()[e[0]] - pGroup.positions0()[e[1]]).norm(),
+                            springStiffness);
+    pGroup.addEnergy(springs);
+    auto anchors = std::make_shared<SpringAnchorEnergy>();
+    for (int id : anchorIds) anchors->addStencil({id}, pGroup.positions()[id], anchorStiffness);
+    pGroup.addEnergy(anchors);
+    return pGroup;
+}
+
+ParticleGroup createTetMeshSolid(const std::vector<Vector3> &vertices, const std::vector<Int4> &tets, Real mass,
+                                 Real young, Real poisson, Real anchorStiffness, const std::vector<int> &anchorIds)
+{
+    const TetrahedralMesh mesh(vertices, vertices, tets);
+    std::vector<Real> volumes(vertices.size(), 0);
+    Real totalVolume = 0;
+    for (const auto &t : tets) {
+        const Real v = tetrahedralVolume(vertices[t[0]], vertices[t[1]], vertices[t[2]], vertices[t[3]]);
+        totalVolume += v;
+        for (int k = 0; k < 4; ++k) volumes[t[k]] += v / 4.0;
+    }
+    const Real density = mass / totalVolume;
+    ParticleGroup pGroup;
+    for (size_t i = 0; i < vertices.size(); ++i) pGroup.addParticle(vertices[i], vertices[i], volumes[i] * density);
+    auto anchors = std::make_shared<SpringAnchorEnergy>();
+    for (int id : anchorIds) anchors->addStencil({id}, pGroup.positions0()[id], anchorStiffness);
+    auto snh = std::make_shared<StableNeoHookeanEnergy>();
+    for (const auto &t : mesh.tets()) snh->addStencil(t, young, poisson);
+    pGroup.addEnergy(anchors);
+    pGroup.addEnergy(snh);
+    snh->preparePrecomputations(pGroup);
+    return pGroup;
+}
+
 std::vector<ParticleGroup> createPatchBatch(int nPatches, int nMin, int nMax, Real muLo, Real muHi, Real kbLo,
                                             Real kbHi, Real mass, Real anchorStiffness, uint64_t seed)
 {

@@ -1,5 +1,6 @@
 // C ABI of the scene builders and of the C++ drop-in solvers (include/spgx_scenes.h).
 #include <memory>
+#include <tuple>
 
 #include "../../csrc/api_internal.h"
 #include "spg/scenes.h"
@@ -18,6 +19,30 @@ spgx_status finish(std::unique_ptr<spgx_scene> s, spgx_scene **out)
     spg::gpu::pack(s->groups, s->packed);
     *out = s.release();
     return SPGX_OK;
+}
+
+// Copies loaded mesh arrays and checks the anchor list.
+template <class Cell>
+bool meshInputs(const double *vertices, int32_t n_vertices, const int32_t *cells, int32_t n_cells, int32_t n_anchors,
+                const int32_t *anchors, std::vector<spg::Vector3> &V, std::vector<Cell> &C, std::vector<int> &ids)
+{
+    constexpr int K = static_cast<int>(std::tuple_size<Cell>::value);
+    if (n_vertices < 1 || n_cells < 1 || !vertices || !cells || n_anchors < 0 || (n_anchors > 0 && !anchors)) {
+        spgx::set_error("invalid mesh arguments");
+        return false;
+    }
+    V.resize(size_t(n_vertices));
+    for (int i = 0; i < n_vertices; ++i) V[i] = {vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2]};
+    C.resize(size_t(n_cells));
+    for (int c = 0; c < n_cells; ++c)
+        for (int k = 0; k < K; ++k) C[c][k] = cells[size_t(c) * K + k];
+    ids.assign(anchors, anchors + n_anchors);
+    for (int id : ids)
+        if (id < 0 || id >= n_vertices) {
+            spgx::set_error("anchor index out of range");
+            return false;
+        }
+    return true;
 }
 
 }  // namespace
@@ -92,6 +117,38 @@ spgx_status spgx_scene_patch_batch(int32_t n_patches, int32_t n_min, int32_t n_m
     }
     auto s = std::make_unique<spgx_scene>();
     s->groups = spg::scenes::createPatchBatch(n_patches, n_min, n_max, mu_lo, mu_hi, kb_lo, kb_hi, mass, anchor_k, seed);
+    return finish(std::move(s), out);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_scene_triangle_mesh(const double *vertices, int32_t n_vertices, const int32_t *faces, int32_t n_faces,
+                                     double mass, double spring_k, double bending_k, double anchor_k,
+                                     int32_t n_anchors, const int32_t *anchors, spgx_scene **out)
+{
+    SPGX_GUARD_BEGIN
+    std::vector<spg::Vector3> V;
+    std::vector<spg::Int3> F;
+    std::vector<int> ids;
+    if (!out || !meshInputs(vertices, n_vertices, faces, n_faces, n_anchors, anchors, V, F, ids))
+        return SPGX_ERR_INVALID_ARG;
+    auto s = std::make_unique<spgx_scene>();
+    s->groups.push_back(spg::scenes::createTriangleMeshShell(V, F, mass, spring_k, bending_k, anchor_k, ids));
+    return finish(std::move(s), out);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_scene_tet_mesh(const double *vertices, int32_t n_vertices, const int32_t *tets, int32_t n_tets,
+                                double mass, double young, double poisson, double anchor_k, int32_t n_anchors,
+                                const int32_t *anchors, spgx_scene **out)
+{
+    SPGX_GUARD_BEGIN
+    std::vector<spg::Vector3> V;
+    std::vector<spg::Int4> T;
+    std::vector<int> ids;
+    if (!out || !meshInputs(vertices, n_vertices, tets, n_tets, n_anchors, anchors, V, T, ids))
+        return SPGX_ERR_INVALID_ARG;
+    auto s = std::make_unique<spgx_scene>();
+    s->groups.push_back(spg::scenes::createTetMeshSolid(V, T, mass, young, poisson, anchor_k, ids));
     return finish(std::move(s), out);
     SPGX_GUARD_END
 }

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -53,6 +54,15 @@ def _lib():
         L.spgx_scene_destroy.argtypes = [vp]
         L.spgx_scene_run_gpu_vbd.argtypes = [vp, C.POINTER(N.VbdParams), i32, C.POINTER(f64)]
         L.spgx_scene_run_gpu_xpbd.argtypes = [vp, C.POINTER(N.XpbdParams), i32, C.POINTER(f64)]
+        pi = C.POINTER(i32)
+        L.spgx_scene_triangle_mesh.argtypes = [C.POINTER(f64), i32, pi, i32, f64, f64, f64, f64, i32, pi,
+                                               C.POINTER(vp)]
+        L.spgx_scene_tet_mesh.argtypes = [C.POINTER(f64), i32, pi, i32, f64, f64, f64, f64, i32, pi, C.POINTER(vp)]
+        L.spgx_load_obj.argtypes = [C.c_char_p, C.POINTER(vp)]
+        L.spgx_load_msh.argtypes = [C.c_char_p, C.POINTER(vp)]
+        L.spgx_mesh_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), pi]
+        L.spgx_mesh_copy.argtypes = [vp, C.POINTER(f64), pi]
+        L.spgx_mesh_destroy.argtypes = [vp]
         _bound = True
     return L
 
@@ -152,3 +162,50 @@ def patch_batch(n_patches=512, n_min=16, n_max=128, seed=2024, mu_lo=1e3, mu_hi=
                 mass=0.1, anchor_k=1e5) -> Scene:
     return _make(_lib().spgx_scene_patch_batch, n_patches, n_min, n_max, mu_lo, mu_hi, kb_lo, kb_hi, mass, anchor_k,
                  seed)
+
+
+def _load(fn, path):
+    h = C.c_void_p()
+    N.check(fn(os.fsencode(path), C.byref(h)))
+    try:
+        nv, nc, k = C.c_int64(), C.c_int64(), C.c_int32()
+        N.check(_lib().spgx_mesh_info(h, C.byref(nv), C.byref(nc), C.byref(k)))
+        V = np.zeros((nv.value, 3))
+        cells = np.zeros((nc.value, k.value), np.int32)
+        N.check(_lib().spgx_mesh_copy(h, V.ctypes.data_as(C.POINTER(C.c_double)),
+                                      cells.ctypes.data_as(C.POINTER(C.c_int32))))
+    finally:
+        _lib().spgx_mesh_destroy(h)
+    return V, cells
+
+
+def load_obj(path):
+    """spg::io::loadObj: (vertices (n, 3) float64 holding float values, triangles (m, 3))."""
+    return _load(_lib().spgx_load_obj, path)
+
+
+def load_msh(path):
+    """spg::io::loadMsh: (nodes (n, 3) float64, tetrahedra (m, 4))."""
+    return _load(_lib().spgx_load_msh, path)
+
+
+def _mesh_args(V, cells, k, anchors):
+    V = np.ascontiguousarray(V, np.float64).reshape(-1, 3)
+    cells = np.ascontiguousarray(cells, np.int32).reshape(-1, k)
+    a = np.ascontiguousarray([] if anchors is None else anchors, np.int32)
+    pi = C.POINTER(C.c_int32)
+    return ((V, cells, a), V.ctypes.data_as(C.POINTER(C.c_double)), len(V), cells.ctypes.data_as(pi), len(cells),
+            len(a), a.ctypes.data_as(pi))
+
+
+def triangle_mesh(V, F, mass=0.1, spring_k=1e4, bending=1e-4, anchor_k=1e5, anchors=None) -> Scene:
+    """A shell on a triangle mesh: springs on every edge, bending on interior edges, anchors."""
+    keep, v, nv, f, nf, na, a = _mesh_args(V, F, 3, anchors)
+    return _make(_lib().spgx_scene_triangle_mesh, v, nv, f, nf, mass, spring_k, bending, anchor_k, na, a)
+
+
+def tet_mesh(V, T, mass=1.0, young=1e6, poisson=0.45, anchor_k=1e4, anchors=None) -> Scene:
+    """A solid on a tetrahedral mesh: Stable Neo-Hookean tets and anchors."""
+    keep, v, nv, t, nt, na, a = _mesh_args(V, T, 4, anchors)
+    return _make(_lib().spgx_scene_tet_mesh, v, nv, t, nt, mass, young, poisson, anchor_k, na, a)
+
