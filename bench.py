@@ -26,6 +26,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -293,6 +295,63 @@ def other_configs(local) -> dict:
                                                "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3)}
     x.close()
     out["mesh_input"] = mesh_input()
+    out["topology_change"] = topology_change(local)
+    return out
+
+
+def topology_change(local) -> dict:
+    """Setup costs on a topology change of the 513x513 cloth: creating a solver (colouring,
+    layout, tiles, with and without the launch autotuner), a pick (dynamic anchor) added
+    between steps, and the energies' precomputations and incidence lists on the host against
+    the GPU. Wall times on the host, median of three."""
+    from spg_gb300 import native as N
+    from spg_gb300 import scenes as S
+
+    def med(fn, reps=3):
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return 1e3 * statistics.median(ts)
+
+    obj = S.spring_cloth(ROWS).objects[0]
+    out = {}
+    kw = dict(dt=DT, iterations=ITERATIONS, gravity=GRAVITY, device=local)
+    t0 = time.perf_counter()
+    s = N.VbdSolver([obj], **kw)
+    out["create_autotuned_ms"] = 1e3 * (time.perf_counter() - t0)
+    k, g, b = s.launch()
+    fixed = dict(kernel=k, lanes_per_vertex=g, block_size=b if k == 1 else 0, tile_vertices=b // g if k >= 2 else 0)
+    s.close()
+
+    def create_fixed():
+        N.VbdSolver([obj], **kw, **fixed).close()
+
+    out["create_fixed_launch_ms"] = med(create_fixed)
+    s = N.VbdSolver([obj], **kw, **fixed)
+    for _ in range(3):
+        s.step()
+    plain = statistics.median(s.step().device_ms for _ in range(3))
+    v = obj.nv - 1
+    x = s.state(0)[0][v]
+    out["pick_add_ms"] = med(lambda: (s.set_picks([(0, v, x + 0.01, 1e4)]), s.set_picks([])))
+    s.set_picks([(0, v, x + 0.01, 1e4)])
+    s.step()
+    picked = statistics.median(s.step().device_ms for _ in range(3))
+    out["step_ms_without_pick"], out["step_ms_with_pick"] = plain, picked
+    s.close()
+    bend = next(e for e in obj.energies if e.type == N.BENDING)
+    springs = next(e for e in obj.energies if e.type == N.SPRING)
+    for name, e, mat in (("bending", bend, [0.0, 1e-4]), ("springs", springs, [0.0, 1e4])):
+        m = np.asarray(mat, np.float64)
+        host = med(lambda: N.precompute_params(e.type, e.stencils, obj.x0, m, device=None))
+        dev = med(lambda: N.precompute_params(e.type, e.stencils, obj.x0, m, device=local))
+        out[f"precompute_{name}"] = {"stencils": e.n, "host_ms": host, "gpu_ms": dev}
+    host = med(lambda: N.incidences(obj))
+    dev = med(lambda: N.incidences(obj, device=local))
+    out["incidences"] = {"entries": int(sum(e.n * e.stencils.shape[1] for e in obj.energies)), "host_ms": host,
+                         "gpu_ms": dev}
     return out
 
 
@@ -307,7 +366,6 @@ def mesh_input() -> dict:
 
     def faces(n):
         """The triangles of the grid builder (alternating diagonals), row by row."""
-        import numpy as np
         r, c = (a.ravel() for a in np.meshgrid(np.arange(1, n), np.arange(1, n), indexing="ij"))
         even = ((r + c) % 2 == 0)[:, None]
         ll, ul, ur, lr = r * n + c - 1, (r - 1) * n + c - 1, (r - 1) * n + c, r * n + c

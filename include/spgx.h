@@ -134,6 +134,39 @@ spgx_status spgx_color_stencils(const spgx_energy_desc *energy, int32_t *colors)
 spgx_status spgx_incidences(const spgx_object_desc *obj, int32_t *counts, int32_t *entries, int64_t *total);
 
 /* ------------------------------------------------------------------------------------ */
+/* Device-side setup for topology changes                                               */
+
+/* Values per stencil that addStencil() takes, for spgx_precompute_params:
+ *   SPRING, SPRING_CONTINUUM, SPRING_SQUARED_CONTINUUM  [restLength, stiffness]
+ *                       (restLength <= 0 takes |x0[s0] - x0[s1]|)
+ *   SPRING_ANCHOR       [anchor.x, anchor.y, anchor.z, stiffness]
+ *   DISCRETE_BENDING, BARAFF_WITKIN_BENDING, QUADRATIC_BENDING  [restTheta, stiffness]
+ *                       (restTheta is validated as addStencil does, then replaced by the rest angle)
+ *   MEMBRANE_STVK, STABLE_NEO_HOOKEAN, STVK, STABLE_SQUARED_NEO_HOOKEAN  [young, poisson]
+ *   MEMBRANE_BARAFF_WITKIN, MEMBRANE_CHOI  [kWeft, kWarp, kBias]
+ *   STATIC_LOAD         [stiffness, direction.x, .y, .z]
+ * Returns 0 for an unknown type. */
+int32_t spgx_material_count(int32_t type);
+/* The energies' addStencil + preparePrecomputations on the GPU: fills params (n_stencils x
+ * spgx_param_count(type), the layout above) from the rest positions x0 (3 * n_vertices) and
+ * per-stencil material values (material_stride doubles apart; 0 = one row for all stencils).
+ * Every value equals the host classes' to the last bit, except the rest angles of the
+ * bending energies (atan2, within a few ulp). A stencil the reference would reject (rest
+ * length, angle, area or volume) fails the call with the reference's message. */
+spgx_status spgx_precompute_params(int32_t type, int32_t n_stencils, const int32_t *stencils, int32_t n_vertices,
+                                   const double *x0, const double *material, int32_t material_stride,
+                                   double *params, int32_t device);
+/* The same on the host, through the host energy classes' addStencil + preparePrecomputations
+ * (the reference's setup path); the baseline spgx_precompute_params replaces. */
+spgx_status spgx_precompute_params_host(int32_t type, int32_t n_stencils, const int32_t *stencils,
+                                        int32_t n_vertices, const double *x0, const double *material,
+                                        int32_t material_stride, double *params);
+/* spgx_incidences computed on the GPU (counting pass, scan, scatter, per-bucket ordering):
+ * the same counts and entries, bit for bit. With counts and entries NULL only *total is set. */
+spgx_status spgx_incidences_device(const spgx_object_desc *obj, int32_t device, int32_t *counts, int32_t *entries,
+                                   int64_t *total);
+
+/* ------------------------------------------------------------------------------------ */
 /* Vertex Block Descent                                                                  */
 
 typedef struct spgx_vbd spgx_vbd;
@@ -219,6 +252,16 @@ spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts,
 /* Launch configuration the solver uses (after autotuning): the kernel (1, 2 or 3), lanes per
  * vertex and threads per CTA. */
 spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *kernel, int32_t *lanes_per_vertex, int32_t *block_size);
+/* Dynamic anchors for interactive picking (apps/solverCompare.cpp:717-726 adds a one-stencil
+ * SpringAnchorEnergy to the picked ParticleGroup, :1524 moves it with updateAnchor, :1499
+ * removes it; each change flags a VBD topology update). Replaces the set of picks: pick q
+ * pulls vertex vertex[q] of object object[q] towards target[3q..3q+2] with stiffness[q], as a
+ * one-stencil SpringAnchorEnergy appended after the object's energies would. Takes effect at
+ * the next step, with no rebuild of colours, incidences or tiles (an anchor adds no graph
+ * edge, so the reference's recolouring gives the same colours). n = 0 removes every pick. */
+#define SPGX_MAX_PICKS 16
+spgx_status spgx_vbd_set_picks(spgx_vbd *h, int32_t n, const int32_t *object, const int32_t *vertex,
+                               const double *target, const double *stiffness);
 /* Runs `iterations` colour sweeps with a CUDA event pair around every colour launch on the
  * handle's stream and writes the mean duration (ms) of each colour's launch to color_ms
  * (spgx_vbd_num_colors(h, -1, ...) entries). Advances the positions like the iterations of

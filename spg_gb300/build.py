@@ -24,6 +24,11 @@ COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contra
           f"-I{os.path.join(ROOT, 'include')}", f"-I{CSRC}", f"-I{os.path.join(HOST, 'include')}"]
 
 
+# Extra flags per translation unit: the setup-time precomputations follow the host's FP64
+# arithmetic operation by operation, so they are compiled without FMA contraction.
+EXTRA = {"precompute.cu": ["--fmad=false"]}
+
+
 def sources() -> list[str]:
     out = []
     for d in (CSRC, os.path.join(HOST, "src")):
@@ -37,9 +42,9 @@ def sources() -> list[str]:
 
 def headers() -> list[str]:
     out = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
-    for d in (CSRC, os.path.join(HOST, "include", "spg"), os.path.join(HOST, "include")):
-        if os.path.isdir(d):
-            out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh"))]
+    for d in (CSRC, os.path.join(HOST, "include")):
+        for dirpath, _, files in os.walk(d):
+            out += [os.path.join(dirpath, f) for f in files if f.endswith((".h", ".cuh"))]
     return [h for h in out if os.path.isfile(h)]
 
 
@@ -70,7 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for s in srcs:
         o = _obj(s)
         if force or _stale(o, [s] + hdrs):
-            extra = ["-x", "cu"] if s.endswith(".cu") else []
+            extra = (["-x", "cu"] if s.endswith(".cu") else []) + EXTRA.get(os.path.basename(s), [])
             jobs.append([NVCC, *ARCH, *COMMON, *extra, "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(_run, jobs))

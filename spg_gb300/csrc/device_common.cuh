@@ -61,7 +61,27 @@ struct DevState {
     int *counters;          // [0] FP64 fallback solves, [1] det-guard skips, [3] learned guesses kept,
                             // [4] extrapolated guesses kept (kCounters ints; [2] is status)
     unsigned int *status;   // bit 0: non-finite update, bit 1: a bounded wait gave up
+    // Dynamic anchors (interactive picking): n_pick one-stencil spring anchors, each pulling
+    // internal vertex pick_v[q] towards pick_a[q].xyz with stiffness pick_a[q].w.
+    int n_pick;
+    const int *pick_v;
+    const float4 *pick_a;
 };
+
+// Adds the dynamic anchors of vertex v (base b, delta d) to a force and Hessian diagonal:
+// f -= k (x - a), H += k I, as SpringAnchorEnergy does for the energy appended last.
+__device__ __forceinline__ void add_picks(const DevState &S, int v, float4 b, float4 d, float &f0, float &f1,
+                                          float &f2, float &hd)
+{
+    for (int q = 0; q < S.n_pick; ++q)
+        if (__ldg(S.pick_v + q) == v) {
+            const float4 a = __ldg(S.pick_a + q);
+            f0 -= a.w * ((b.x - a.x) + d.x);
+            f1 -= a.w * ((b.y - a.y) + d.y);
+            f2 -= a.w * ((b.z - a.z) + d.z);
+            hd += a.w;
+        }
+}
 
 typedef Vec3<float> V3f;
 

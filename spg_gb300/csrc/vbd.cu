@@ -31,11 +31,13 @@ __device__ __forceinline__ void solve_and_update(const DevState &S, int v, const
                                                  float4 tg, float invdt2, float fb2)
 {
     const float c = tg.w * invdt2;
-    const float f0 = acc.f[0] - c * (d4.x - tg.x);
-    const float f1 = acc.f[1] - c * (d4.y - tg.y);
-    const float f2 = acc.f[2] - c * (d4.z - tg.z);
-    const float h0 = acc.h[0] + c, h1 = acc.h[1], h2 = acc.h[2];
-    const float h3 = acc.h[3] + c, h4 = acc.h[4], h5 = acc.h[5] + c;
+    float f0 = acc.f[0] - c * (d4.x - tg.x);
+    float f1 = acc.f[1] - c * (d4.y - tg.y);
+    float f2 = acc.f[2] - c * (d4.z - tg.z);
+    float hd = c;
+    if (S.n_pick) add_picks(S, v, S.pos[2 * v], d4, f0, f1, f2, hd);
+    const float h0 = acc.h[0] + hd, h1 = acc.h[1], h2 = acc.h[2];
+    const float h3 = acc.h[3] + hd, h4 = acc.h[4], h5 = acc.h[5] + hd;
     const float s = fmaxf(fmaxf(fmaxf(fabsf(h0), fabsf(h1)), fmaxf(fabsf(h2), fabsf(h3))), fmaxf(fabsf(h4), fabsf(h5)));
     float dx = 0.f, dy = 0.f, dz = 0.f;
     bool apply = false;
@@ -302,6 +304,10 @@ __global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileV
     double r2 = 0.0;
     if (active && lane == 0) {
         const float4 tg = tv.tg;
+        if (S.n_pick) {
+            float hd = 0.f;
+            add_picks(S, h0.x + lv, sb[lv], sd[lv], acc.f[0], acc.f[1], acc.f[2], hd);
+        }
         const double c = double(tg.w) * invdt2;
         const double rx = c * (double(cx.ds.x) - tg.x) - acc.f[0];
         const double ry = c * (double(cx.ds.y) - tg.y) - acc.f[1];
@@ -334,6 +340,10 @@ __global__ void __launch_bounds__(256) residual_kernel(const DevTables T, const 
     double r2 = 0.0;
     if (active && lane == 0) {
         const float4 tg = S.tgt[v];
+        if (S.n_pick) {
+            float hd = 0.f;
+            add_picks(S, v, S.pos[2 * v], S.pos[2 * v + 1], acc.f[0], acc.f[1], acc.f[2], hd);
+        }
         const double c = double(tg.w) * invdt2;
         const double rx = c * (double(ds.x) - tg.x) - acc.f[0];
         const double ry = c * (double(ds.y) - tg.y) - acc.f[1];
@@ -604,6 +614,11 @@ spgx_status VbdSolver::init(const spgx_scene_desc *scene, const spgx_vbd_params 
     S.adj = d_adj.as<int>();
     S.counters = d_counters.as<int>();
     S.status = reinterpret_cast<unsigned int *>(d_counters.as<int>() + 2);
+    SPGX_TRY_STATUS(d_pick_v.alloc(SPGX_MAX_PICKS * sizeof(int)));
+    SPGX_TRY_STATUS(d_pick_a.alloc(SPGX_MAX_PICKS * sizeof(float4)));
+    S.n_pick = 0;
+    S.pick_v = d_pick_v.as<int>();
+    S.pick_a = d_pick_a.as<float4>();
     SPGX_TRY_STATUS(setup_tiles(P.tile_vertices ? P.tile_vertices : kTileCandidates[0]));
     SPGX_TRY_STATUS(setup_flow());
     SPGX_TRY_STATUS(configure_launch());
@@ -905,6 +920,35 @@ spgx_status VbdSolver::configure_launch()
     kernel = pick.kernel;
     lanes = pick.lanes;
     block = pick.block;
+    return SPGX_OK;
+}
+
+spgx_status VbdSolver::set_picks(int n, const int32_t *object, const int32_t *vertex, const double *target,
+                                 const double *k)
+{
+    if (n < 0 || n > SPGX_MAX_PICKS || (n > 0 && (!object || !vertex || !target || !k))) {
+        set_error("picks: 0 to SPGX_MAX_PICKS anchors with object, vertex, target and stiffness");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    int vi[SPGX_MAX_PICKS];
+    float4 a[SPGX_MAX_PICKS];
+    for (int q = 0; q < n; ++q) {
+        if (object[q] < 0 || object[q] >= static_cast<int>(L.objects.size()) || vertex[q] < 0 ||
+            vertex[q] >= L.objects[object[q]].nv) {
+            set_error("pick " + std::to_string(q) + " names no vertex of the scene");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        vi[q] = L.ext2int[L.objects[object[q]].vertex_base + vertex[q]];
+        a[q] = make_float4(float(target[3 * q]), float(target[3 * q + 1]), float(target[3 * q + 2]), float(k[q]));
+    }
+    if (n > 0) {
+        SPGX_CUDA(cudaMemcpyAsync(d_pick_v.as<int>(), vi, n * sizeof(int), cudaMemcpyHostToDevice, stream));
+        SPGX_CUDA(cudaMemcpyAsync(d_pick_a.as<float4>(), a, n * sizeof(float4), cudaMemcpyHostToDevice, stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+    }
+    // The count is a kernel argument (captured in the step graph); the slots are read live.
+    if (S.n_pick != n) graph_valid = false;
+    S.n_pick = n;
     return SPGX_OK;
 }
 
@@ -1359,6 +1403,19 @@ spgx_status spgx_vbd_get_adjacency(spgx_vbd *h, int32_t object, int32_t *counts,
     if (counts) std::copy(O.adj_counts.begin(), O.adj_counts.end(), counts);
     if (entries) std::copy(O.adj_entries.begin(), O.adj_entries.end(), entries);
     return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_set_picks(spgx_vbd *h, int32_t n, const int32_t *object, const int32_t *vertex,
+                               const double *target, const double *stiffness)
+{
+    SPGX_GUARD_BEGIN
+    if (!h) {
+        spgx::set_error("NULL solver handle");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_CUDA(cudaSetDevice(h->s->device));
+    return h->s->set_picks(n, object, vertex, target, stiffness);
     SPGX_GUARD_END
 }
 

@@ -52,6 +52,7 @@ struct VbdSolver {
     mutable int flow_epoch{0};    // sweeps the dataflow kernel has completed on this handle
     mutable cudaError_t flow_launch_error{cudaSuccess};
     WarmStart W;
+    DevBuf d_pick_v, d_pick_a;  // dynamic anchors, SPGX_MAX_PICKS slots
 
     VbdSolver() = default;
     VbdSolver(const VbdSolver &) = delete;
@@ -76,6 +77,8 @@ struct VbdSolver {
     spgx_status upload_state();
     spgx_status set_warm_start(const Mlp *mlp, int mode);
     void launch_warm(cudaStream_t st);
+    // Replaces the dynamic anchors (picking) between steps.
+    spgx_status set_picks(int n, const int32_t *object, const int32_t *vertex, const double *target, const double *k);
 };
 
 }  // namespace spgx

@@ -21,8 +21,9 @@ struct PackedObject {
     spgx_object_desc desc{};
 };
 
-// Throws std::runtime_error naming the energy if its type is not one of the five supported.
-void pack(const ParticleGroup &pGroup, PackedObject &out);
+// Throws std::runtime_error naming the energy if its type is not supported. With nEnergies >= 0
+// only the group's first nEnergies energies are packed.
+void pack(const ParticleGroup &pGroup, PackedObject &out, int nEnergies = -1);
 
 struct PackedScene {
     std::vector<PackedObject> objects;
@@ -30,6 +31,7 @@ struct PackedScene {
     spgx_scene_desc desc{};
 };
 
-void pack(const std::vector<ParticleGroup> &groups, PackedScene &out);
+// nEnergies: per group, as above (empty = every energy).
+void pack(const std::vector<ParticleGroup> &groups, PackedScene &out, const std::vector<int> &nEnergies = {});
 
 }  // namespace spg::gpu

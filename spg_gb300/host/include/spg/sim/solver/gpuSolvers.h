@@ -53,15 +53,28 @@ public:
     void setIterations(int iterations);
     void setTolerance(Real relativeResidual, int maxIterations, int checkInterval = 10);
     void setLaunch(int lanesPerVertex, int blockSize);
+    // 0 = autotune, 1 = lanes kernel, 2 = tile kernel, 3 = dataflow kernel; tile size 0 = autotune.
+    void setKernel(int kernel, int tileVertices = 0);
     // Pushes host-side edits of positions/velocities to the device before the next step.
     void markHostStateDirty() { m_hostDirty = true; }
     const spgx_step_stats &lastStats() const { return m_stats; }
     spgx_vbd *handle() { return m_handle; }
 
 private:
+    struct Pick {
+        int object;
+        const SpringAnchorEnergy *energy;
+    };
+    // Splits every group's energies into the packed prefix and the trailing one-stencil
+    // SpringAnchorEnergy objects (at most SPGX_MAX_PICKS in all), which run as dynamic anchors.
+    void classify(std::vector<int> &packed, std::vector<Pick> &picks) const;
     void prepare();
+    void uploadPicks();
     void pushState();
     void pullState();
+    std::vector<std::vector<const void *>> m_packedEnergies;  // identity of the packed energies
+    std::vector<Pick> m_picks;
+    std::vector<double> m_pickData;  // targets and stiffnesses last uploaded
     InitialGuessType m_initialGuessType{InitialGuessType::InertialWithAcceleration};
     spgx_vbd_params m_params{};
     spgx_vbd *m_handle{nullptr};

@@ -1,5 +1,6 @@
 // Packing of ParticleGroups into the C ABI descriptor (spgx_object_desc): the reference's
 // accessors for each energy's precomputed per-stencil data, in the order spgx.h documents.
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 #include <typeinfo>
@@ -37,7 +38,7 @@ static void pack_membrane(const E &en, std::vector<double> &p, const char *name)
     }
 }
 
-void pack(const ParticleGroup &g, PackedObject &out)
+void pack(const ParticleGroup &g, PackedObject &out, int nEnergies)
 {
     const int nv = g.size();
     out = PackedObject();
@@ -49,8 +50,10 @@ void pack(const ParticleGroup &g, PackedObject &out)
             out.x[3 * i + a] = g.positions()[i][a];
             out.v[3 * i + a] = g.velocities()[i][a];
         }
-    for (const auto &ep : g.energies()) {
-        const auto *e = ep.get();
+    const int ne = nEnergies < 0 ? static_cast<int>(g.energies().size())
+                                  : std::min(nEnergies, static_cast<int>(g.energies().size()));
+    for (int ei = 0; ei < ne; ++ei) {
+        const auto *e = g.energies()[ei].get();
         std::vector<int32_t> st;
         for (int s : e->flatStencils()) st.push_back(s);
         std::vector<double> p;
@@ -146,13 +149,13 @@ void pack(const ParticleGroup &g, PackedObject &out)
                 out.energies.data()};
 }
 
-void pack(const std::vector<ParticleGroup> &groups, PackedScene &out)
+void pack(const std::vector<ParticleGroup> &groups, PackedScene &out, const std::vector<int> &nEnergies)
 {
     out.objects.clear();
     out.objects.resize(groups.size());
     out.descs.clear();
     for (size_t i = 0; i < groups.size(); ++i) {
-        pack(groups[i], out.objects[i]);
+        pack(groups[i], out.objects[i], i < nEnergies.size() ? nEnergies[i] : -1);
         out.descs.push_back(out.objects[i].desc);
     }
     out.desc = {static_cast<int32_t>(out.descs.size()), out.descs.data()};

@@ -104,6 +104,7 @@ def lib():
         L.spgx_vbd_get_colors.argtypes = [vp, i32, ip]
         L.spgx_vbd_get_adjacency.argtypes = [vp, i32, ip, ip, C.POINTER(C.c_int64)]
         L.spgx_vbd_get_launch.argtypes = [vp, ip, ip, ip]
+        L.spgx_vbd_set_picks.argtypes = [vp, i32, ip, ip, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.spgx_vbd_profile_sweeps.argtypes = [vp, i32, dp]
         L.spgx_eval_vertex_blocks.argtypes = [i32, i32, dp, dp, ip, dp, dp]
         L.spgx_eval_constraints.argtypes = [i32, i32, dp, dp, dp, dp]
@@ -119,6 +120,13 @@ def lib():
         L.spgx_color_vertices.argtypes = [C.POINTER(ObjectDesc), ip]
         L.spgx_color_stencils.argtypes = [C.POINTER(EnergyDesc), ip]
         L.spgx_incidences.argtypes = [C.POINTER(ObjectDesc), ip, ip, C.POINTER(C.c_int64)]
+        L.spgx_incidences_device.argtypes = [C.POINTER(ObjectDesc), i32, ip, ip, C.POINTER(C.c_int64)]
+        L.spgx_material_count.restype = i32
+        L.spgx_material_count.argtypes = [i32]
+        L.spgx_precompute_params.argtypes = [i32, i32, ip, i32, C.POINTER(C.c_double), C.POINTER(C.c_double), i32,
+                                             C.POINTER(C.c_double), i32]
+        L.spgx_precompute_params_host.argtypes = [i32, i32, ip, i32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                  i32, C.POINTER(C.c_double)]
         fp = C.POINTER(C.c_float)
         L.spgx_mlp_num_params.restype = i32
         L.spgx_mlp_create.argtypes = [C.c_uint64, i32, C.POINTER(vp)]
@@ -294,6 +302,17 @@ class VbdSolver:
         out = np.zeros(sum(self.objects_nv), np.int32)
         check(lib().spgx_vbd_get_vertex_order(self.h, _p(out, C.c_int32)))
         return out
+
+    def set_picks(self, picks):
+        """Dynamic anchors for picking: a list of (object, vertex, target xyz, stiffness)."""
+        n = len(picks)
+        o = np.array([p[0] for p in picks], np.int32).reshape(-1)
+        v = np.array([p[1] for p in picks], np.int32).reshape(-1)
+        t = np.array([p[2] for p in picks], np.float64).reshape(-1)
+        k = np.array([p[3] for p in picks], np.float64).reshape(-1)
+        o, v, t, k = (np.ascontiguousarray(a) for a in (o, v, t, k))
+        check(lib().spgx_vbd_set_picks(self.h, n, _p(o, C.c_int32), _p(v, C.c_int32), _p(t, C.c_double),
+                                       _p(k, C.c_double)))
 
     def launch(self):
         """(kernel, lanes_per_vertex or tile vertices, block size) chosen by the solver."""
@@ -511,13 +530,38 @@ def color_stencils(energy) -> np.ndarray:
     return out[:n]
 
 
-def incidences(obj):
-    """Reference-order incidence lists: counts (V, n_energies) and (stencil, slot) pairs."""
+def incidences(obj, device=None):
+    """Reference-order incidence lists: counts (V, n_energies) and (stencil, slot) pairs,
+    computed on the host, or on the GPU `device` when given."""
     d = Descriptor([obj])
     ob = d.scene.objects[0]
     tot = C.c_int64()
-    check(lib().spgx_incidences(C.byref(ob), None, None, C.byref(tot)))
+    if device is None:
+        fn = lambda c, e: lib().spgx_incidences(C.byref(ob), c, e, C.byref(tot))  # noqa: E731
+    else:
+        fn = lambda c, e: lib().spgx_incidences_device(C.byref(ob), device, c, e, C.byref(tot))  # noqa: E731
+    check(fn(None, None))
     counts = np.zeros(max(1, ob.n_vertices * ob.n_energies), np.int32)
     ent = np.zeros((max(1, tot.value), 2), np.int32)
-    check(lib().spgx_incidences(C.byref(ob), _p(counts, C.c_int32), _p(ent, C.c_int32), C.byref(tot)))
+    check(fn(_p(counts, C.c_int32), _p(ent, C.c_int32)))
     return counts[:ob.n_vertices * ob.n_energies].reshape(ob.n_vertices, ob.n_energies), ent[:tot.value]
+
+
+def precompute_params(etype, stencils, x0, material, device=0):
+    """The energy's addStencil + preparePrecomputations on the GPU `device` (None: on the host
+    through the host energy classes): packed params (n, P) from the rest positions and the
+    per-stencil material values (one row, or one per stencil)."""
+    st = np.ascontiguousarray(stencils, np.int32).reshape(-1, STENCIL_SIZE[etype])
+    x0 = np.ascontiguousarray(x0, np.float64).reshape(-1, 3)
+    m = np.ascontiguousarray(material, np.float64)
+    M = lib().spgx_material_count(etype)
+    stride = 0 if m.ndim == 1 else M
+    m = m.reshape(-1, M)
+    out = np.zeros((len(st), PARAM_COUNT[etype]))
+    args = (etype, len(st), _p(st, C.c_int32), len(x0), _p(x0, C.c_double), _p(m, C.c_double), stride,
+            _p(out, C.c_double))
+    if device is None:
+        check(lib().spgx_precompute_params_host(*args))
+    else:
+        check(lib().spgx_precompute_params(*args, device))
+    return out

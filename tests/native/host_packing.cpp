@@ -21,6 +21,42 @@ extern "C" int host_pack(int type, int nv, const double *x0, int n_stencils, con
         }
         std::shared_ptr<Energy<ParticleGroup>> e;
         switch (type) {
+        case SPGX_ENERGY_SPRING: {
+            auto en = std::make_shared<SpringEnergy>();
+            for (int s = 0; s < n_stencils; ++s) {
+                const Vector3 d = g.positions0()[stencils[2 * s]] - g.positions0()[stencils[2 * s + 1]];
+                en->addStencil({stencils[2 * s], stencils[2 * s + 1]}, d.norm(), a[0]);
+            }
+            e = en;
+            break;
+        }
+        case SPGX_ENERGY_SPRING_ANCHOR: {
+            auto en = std::make_shared<SpringAnchorEnergy>();
+            for (int s = 0; s < n_stencils; ++s) en->addStencil({stencils[s]}, g.positions0()[stencils[s]], a[0]);
+            e = en;
+            break;
+        }
+        case SPGX_ENERGY_DISCRETE_BENDING: {
+            auto en = std::make_shared<DiscreteBendingEnergy>();
+            for (int s = 0; s < n_stencils; ++s)
+                en->addStencil({stencils[4 * s], stencils[4 * s + 1], stencils[4 * s + 2], stencils[4 * s + 3]}, 0.0, a[0]);
+            e = en;
+            break;
+        }
+        case SPGX_ENERGY_MEMBRANE_STVK: {
+            auto en = std::make_shared<MembraneStvkEnergy>();
+            for (int s = 0; s < n_stencils; ++s)
+                en->addStencil({stencils[3 * s], stencils[3 * s + 1], stencils[3 * s + 2]}, a[0], a[1]);
+            e = en;
+            break;
+        }
+        case SPGX_ENERGY_STABLE_NEO_HOOKEAN: {
+            auto en = std::make_shared<StableNeoHookeanEnergy>();
+            for (int s = 0; s < n_stencils; ++s)
+                en->addStencil({stencils[4 * s], stencils[4 * s + 1], stencils[4 * s + 2], stencils[4 * s + 3]}, a[0], a[1]);
+            e = en;
+            break;
+        }
         case SPGX_ENERGY_STVK: {
             auto en = std::make_shared<StvkEnergy>();
             for (int s = 0; s < n_stencils; ++s)
