@@ -289,6 +289,18 @@ def other_configs(local) -> dict:
                                               "converged": [bool(st.converged) for st in stats],
                                               "precision": "FP64 assembly and CG"}
     imp.close()
+    names = ["newton_dx", "newton_dv", "newton_robust", "baraff_witkin", "bdf2", "static_newton",
+             "quasi_static_newton", "quasi_static_newton_robust", "symplectic_euler"]
+    solvers = {}
+    for method, name in enumerate(names):
+        dt = 1e-4 if name == "symplectic_euler" else 1 / 60
+        imp = N.ImplicitSolver([beam], dt=dt, substeps=1, gravity=GRAVITY, device=local, method=method)
+        stats = [imp.step() for _ in range(5)][2:]
+        solvers[name] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
+                         "cg_iterations": [int(st.iterations) for st in stats]}
+        imp.close()
+    out["global_solvers_snh_beam_41x11x11"] = {"dt": "1/60 s (symplectic Euler 1e-4 s)", "precision": "FP64",
+                                               "solvers": solvers}
     x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local)
     ms = statistics.mean(_timed_steps(x, 5))
     out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,

@@ -359,14 +359,40 @@ spgx_status spgx_eval_constraints(int32_t type, int32_t n, const double *X, cons
 int32_t spgx_num_constraints(int32_t type);
 
 /* ------------------------------------------------------------------------------------ */
-/* Implicit Euler, one Newton step per substep (spg::solver::ImplicitEulerNewtonDx,
- * implicitEulerNewtonDx.cpp:11-65, with ImplicitEulerBase's system force, stiffness matrix
- * and conjugate-gradient solve, implicitEulerBase.cpp:102-240). Per substep: y = x + h v,
- * f = M g - grad E(y), solve (M / h^2 + hess E(y)) dx = f by conjugate gradients with the
- * diagonal preconditioner, x = y + dx, v = (x - x0) / h. Every energy type is accepted; the
- * element Hessians are the full ones (no definiteness projection), as in the reference.
- * spgx_step_stats: iterations = CG iterations summed over substeps, residual_final = the
- * last solve's relative residual |r| / |f|, converged = every solve reached cg_threshold. */
+/* The global solvers of the reference (spg/source/sim/solver/), on ImplicitEulerBase's system
+ * force, stiffness matrix and conjugate-gradient solve (implicitEulerBase.cpp:102-240):
+ * f = M g - grad E(x), K = -hess E(x) (full element Hessians, no definiteness projection),
+ * linear systems by CG with the diagonal preconditioner (relative tolerance cg_threshold,
+ * cg_max_iterations, zero start). State, assembly and solve are FP64. Per substep of h:
+ *   NEWTON_DX       implicitEulerNewtonDx.cpp:31-55     x += v h; (M/h^2 - K) dx = f; x += dx; v = (x - x0)/h
+ *   NEWTON_DV       implicitEulerNewtonDv.cpp:31-60     x += v h; (M - h^2 K) dv = h f; v = v0 + dv; x = x0 + v h
+ *   NEWTON_ROBUST   implicitEulerNewtonRobust.cpp:33-126 Newton on (M - h^2 K) dv = h f - M (v_i - v0) with a
+ *                   halving line search (5 steps), 5 iterations, threshold 1e-5; a failed substep restores
+ *                   x0, v0 and scales the persistent step by 0.75; more than 5 successes in a row grow it back
+ *   BARAFF_WITKIN   implicitEulerBaraffWitkin.cpp:31-52 (M - h^2 K) dv = h (f + h K v0); v = v0 + dv; x += v h
+ *   BDF2            bdf2.cpp:31-74                      (M - 4/9 h^2 K) dv = 1/3 M (v0 - v_-1)
+ *                   + 2/3 h (f + 1/3 K (x0 - x_-1 + 2 h v0)); v = v0 + dv; x = 4/3 x0 - 1/3 x_-1 + 2/3 v h
+ *   STATIC_NEWTON   staticNewton.cpp:30-45              K dx = -f; x += dx
+ *   QUASI_STATIC_NEWTON quasiStaticNewton.cpp:32-49     (M - h^2 K) dx = h^2 f; x += dx
+ *   QUASI_STATIC_NEWTON_ROBUST quasiStaticNewtonRobust.cpp:33-136 Newton on (M/h^2 - K) dx = f - M v/h,
+ *                   v = (x - x0)/h, line search and step control as NEWTON_ROBUST, threshold 1e-2
+ *   SYMPLECTIC_EULER simplecticEuler.cpp:11-62          v += h g + h W (-grad E); x += v h
+ * Every energy type is accepted. spgx_step_stats: iterations = CG iterations summed over
+ * substeps; converged = every solve reached cg_threshold (robust methods: every substep
+ * succeeded); residual_final = the last solve's relative residual |r| / |b| (robust methods:
+ * the last Newton residual norm, residual_initial the first); fallback_solves = Newton
+ * iterations and skipped_solves = failed substeps (robust methods). */
+typedef enum spgx_implicit_method {
+    SPGX_IMPLICIT_NEWTON_DX = 0,          /* spg::solver::ImplicitEulerNewtonDx */
+    SPGX_IMPLICIT_NEWTON_DV = 1,          /* spg::solver::ImplicitEulerNewtonDv */
+    SPGX_IMPLICIT_NEWTON_ROBUST = 2,      /* spg::solver::ImplicitEulerNewtonRobust */
+    SPGX_IMPLICIT_BARAFF_WITKIN = 3,      /* spg::solver::ImplicitEulerBaraffWitkin */
+    SPGX_IMPLICIT_BDF2 = 4,               /* spg::solver::BDF2 */
+    SPGX_STATIC_NEWTON = 5,               /* spg::solver::StaticNewton */
+    SPGX_QUASI_STATIC_NEWTON = 6,         /* spg::solver::QuasiStaticNewton */
+    SPGX_QUASI_STATIC_NEWTON_ROBUST = 7,  /* spg::solver::QuasiStaticNewtonRobust */
+    SPGX_SYMPLECTIC_EULER = 8             /* spg::solver::SimplecticEuler */
+} spgx_implicit_method;
 
 typedef struct spgx_implicit spgx_implicit;
 
@@ -377,6 +403,7 @@ typedef struct spgx_implicit_params {
     double cg_threshold;       /* ImplicitEulerBase::m_cgThreshold (1e-5) */
     int32_t cg_max_iterations; /* ImplicitEulerBase::m_cgMaxIterations (300) */
     int32_t device;
+    int32_t method;            /* spgx_implicit_method (default NEWTON_DX) */
 } spgx_implicit_params;
 
 void spgx_implicit_params_default(spgx_implicit_params *p);
@@ -387,6 +414,8 @@ spgx_status spgx_implicit_step(spgx_implicit *h, spgx_step_stats *stats);
 spgx_status spgx_implicit_get_state(spgx_implicit *h, int32_t object, double *x, double *v);
 spgx_status spgx_implicit_set_state(spgx_implicit *h, int32_t object, const double *x, const double *v);
 spgx_status spgx_implicit_reset(spgx_implicit *h);
+/* The robust methods' current substep (m_currentDt; -1 before the first step). */
+spgx_status spgx_implicit_get_step_size(spgx_implicit *h, double *dt);
 
 /* ------------------------------------------------------------------------------------ */
 /* XPBD (one projection sweep per substep, xpbd.h:13-15)                                  */

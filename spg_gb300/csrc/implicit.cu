@@ -1,21 +1,39 @@
-// GB300 implicit Euler (one Newton step per substep), the GPU counterpart of
-// spg::solver::ImplicitEulerNewtonDx::step (spg/source/sim/solver/implicitEulerNewtonDx.cpp:11-65)
-// with the system assembly and linear solve of ImplicitEulerBase
-// (spg/source/sim/solver/implicitEulerBase.cpp:102-240):
+// GB300 global solvers of SPG: the implicit Euler family, BDF2, static and quasi-static Newton
+// and symplectic Euler (spg/source/sim/solver/), on ImplicitEulerBase's system assembly and
+// linear solve (implicitEulerBase.cpp:102-240):
 //
-//   per substep: x0 = x; y = x + h v (integrateVelocities, particleGroup.cpp:57-63);
-//   f = M g - grad E(y) (getSystemForce); K = -hess E(y) (getSystemStiffnessMatrix, full element
-//   Hessians, no definiteness projection); solve (M / h^2 - K) dx = f by conjugate gradients
-//   with the diagonal preconditioner (Eigen::ConjugateGradient: relative tolerance 1e-5,
-//   300 iterations); x = y + dx; v = (x - x0) / h.
+//   f = M g - grad E(x) (getSystemForce); K = -hess E(x) (getSystemStiffnessMatrix, full
+//   element Hessians, no definiteness projection); linear systems alpha M - beta K solved by
+//   conjugate gradients with the diagonal preconditioner (Eigen::ConjugateGradient: relative
+//   tolerance 1e-5, 300 iterations, zero initial guess).
+//
+// Per substep of step h (each method's step(), restated operation by operation):
+//   NewtonDx (implicitEulerNewtonDx.cpp:31-55): x0 = x; x += v h; solve (M/h^2 - K) dx = f;
+//     x += dx; v = (x - x0) / h.
+//   NewtonDv (implicitEulerNewtonDv.cpp:31-60): x += v h; solve (M - h^2 K) dv = h f;
+//     v = v0 + dv; x = x0 + v h.
+//   NewtonRobust (implicitEulerNewtonRobust.cpp:33-126): Newton iterations on
+//     (M - h^2 K) dv = h f - M (v_i - v0) with a halving line search on the residual norm,
+//     up to 5 iterations and 5 line-search steps; a failed substep restores x0, v0 and scales
+//     the step by 0.75, more than 5 successes in a row grow it back (the step persists).
+//   BaraffWitkin (implicitEulerBaraffWitkin.cpp:31-52): solve (M - h^2 K) dv = h (f + h K v0);
+//     v = v0 + dv; x += v h.
+//   BDF2 (bdf2.cpp:31-74): solve (M - 4/9 h^2 K) dv = 1/3 M (v0 - v-1)
+//     + 2/3 h (f + 1/3 K (x0 - x-1 + 2 h v0)); v = v0 + dv; x = 4/3 x0 - 1/3 x-1 + 2/3 v h.
+//   StaticNewton (staticNewton.cpp:30-45): solve K dx = -f; x += dx.
+//   QuasiStaticNewton (quasiStaticNewton.cpp:32-49): solve (M - h^2 K) dx = h^2 f; x += dx.
+//   QuasiStaticNewtonRobust (quasiStaticNewtonRobust.cpp:33-136): Newton iterations on
+//     (M/h^2 - K) dx = f - M v / h, v = (x - x0) / h, with the same line search and step
+//     control (threshold 1e-2).
+//   SimplecticEuler (simplecticEuler.cpp:11-62): v += h g; v += h W (-grad E); x += v h.
 //
 // Layout: the global matrix is block-sparse with 3x3 blocks (BSR) over the vertex adjacency of
 // all stencils; one thread per element computes the element's gradient and Hessian blocks by
 // forward-mode differentiation over vertex pairs (6 seeded coordinates) and adds them with
-// atomics. Assembly, parameters and the CG run in FP64 (the positions stay FP32 base + delta):
-// a flat cloth at rest has no transverse stiffness, and FP32 rounding of 1 - L0 / |x1 - x0|
-// would add some of the order of the M / h^2 term and change the solution. This solver is off
-// the VBD hot path, so FP64's lower rate is acceptable here.
+// atomics. State, assembly, parameters and the CG are FP64: a flat cloth at rest has no
+// transverse stiffness, and FP32 rounding of 1 - L0 / |x1 - x0| would add some of the order of
+// the M / h^2 term and change the solution. These solvers are off the VBD hot path, so FP64's
+// lower rate is acceptable here.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,28 +75,24 @@ __device__ __forceinline__ void atomic_force(double *f, int v, double gx, double
     atomicAdd(f + 3 * v + 2, -gz);
 }
 
-// Position of vertex j relative to (b0, d0), in FP64 from the FP32 base/delta pairs.
-__device__ __forceinline__ Vec3<double> rel64(const float4 *pos, int j, float4 b0, float4 d0)
-{
-    const float4 b = pos[2 * j], d = pos[2 * j + 1];
-    return mk((double(b.x) - b0.x) + (double(d.x) - d0.x), (double(b.y) - b0.y) + (double(d.y) - d0.y),
-              (double(b.z) - b0.z) + (double(d.z) - d0.z));
-}
-
-// Gradient and Hessian blocks of one element at the current positions, added to the forces
-// (f -= grad) and to the matrix (val += hess).
-template <int S>
-__device__ void assemble_element(const ImplicitTables &T, const float4 *__restrict__ pos, double *force, int e,
+// Gradient and Hessian blocks of one element at the positions x (FP64, 3 per vertex), added to
+// the forces (f -= grad) and, with kHess, to the matrix (val += hess). Positions enter
+// relative to the element's first vertex (the energies are translation invariant).
+template <int S, bool kHess>
+__device__ void assemble_element(const ImplicitTables &T, const double *__restrict__ x, double *force, int e,
                                  int4 ix, int4 info)
 {
     const int iv[4] = {ix.x, ix.y, ix.z, ix.w};
     const double *prm = T.prm + info.y;
     const int type = info.x;
     const int *eb = T.eblk + size_t(e) * 16;
-    const float4 b0 = pos[2 * iv[0]], d0 = pos[2 * iv[0] + 1];
+    const double *x0 = x + 3 * size_t(iv[0]);
     Vec3<double> p[S];
 #pragma unroll
-    for (int j = 0; j < S; ++j) p[j] = rel64(pos, iv[j], b0, d0);
+    for (int j = 0; j < S; ++j) {
+        const double *xj = x + 3 * size_t(iv[j]);
+        p[j] = mk(xj[0] - x0[0], xj[1] - x0[1], xj[2] - x0[2]);
+    }
     if (type == SPGX_ENERGY_QUADRATIC_BENDING) {
         // C = sum_s c_s x_s (linear): grad_a = k c_a C, hess_ab = k c_a c_b I.
         Vec3<double> C = mk(0.0, 0.0, 0.0);
@@ -88,12 +102,13 @@ __device__ void assemble_element(const ImplicitTables &T, const float4 *__restri
 #pragma unroll
         for (int a = 0; a < S; ++a) {
             atomic_force(force, iv[a], k * prm[a] * C.x, k * prm[a] * C.y, k * prm[a] * C.z);
+            if (kHess)
 #pragma unroll
-            for (int b = 0; b < S; ++b) {
-                const double s = k * prm[a] * prm[b];
-                const double H[9] = {s, 0.0, 0.0, 0.0, s, 0.0, 0.0, 0.0, s};
-                atomic_block(T.val, eb[a * S + b], H);
-            }
+                for (int b = 0; b < S; ++b) {
+                    const double s = k * prm[a] * prm[b];
+                    const double H[9] = {s, 0.0, 0.0, 0.0, s, 0.0, 0.0, 0.0, s};
+                    atomic_block(T.val, eb[a * S + b], H);
+                }
         }
         return;
     }
@@ -104,44 +119,52 @@ __device__ void assemble_element(const ImplicitTables &T, const float4 *__restri
     for (int a = 0; a < S; ++a)
 #pragma unroll
         for (int b = a + 1; b < S; ++b) {
+            const bool diag_a = b == a + 1;
+            const bool diag_b = a == S - 2 && b == S - 1;
+            if (!kHess && !diag_a && !diag_b) continue;
             V3A<double, 6> q[S];
             seed_positions<double, S, 6>(p, a, q, b);
             const VAD<double, 6> E = energy_ad(type, q, prm);
-            double Hab[9], Hba[9];
-#pragma unroll
-            for (int r = 0; r < 3; ++r)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    Hab[3 * r + c] = E.h[hidx<6>(r, 3 + c)];
-                    Hba[3 * c + r] = Hab[3 * r + c];
-                }
-            atomic_block(T.val, eb[a * S + b], Hab);
-            atomic_block(T.val, eb[b * S + a], Hba);
-            const bool diag_a = b == a + 1;
-            const bool diag_b = a == S - 2 && b == S - 1;
-            if (diag_a) {
-                double H[9];
+            if (kHess) {
+                double Hab[9], Hba[9];
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) H[3 * r + c] = E.h[r <= c ? hidx<6>(r, c) : hidx<6>(c, r)];
-                atomic_block(T.val, eb[a * S + a], H);
+                    for (int c = 0; c < 3; ++c) {
+                        Hab[3 * r + c] = E.h[hidx<6>(r, 3 + c)];
+                        Hba[3 * c + r] = Hab[3 * r + c];
+                    }
+                atomic_block(T.val, eb[a * S + b], Hab);
+                atomic_block(T.val, eb[b * S + a], Hba);
+            }
+            if (diag_a) {
+                if (kHess) {
+                    double H[9];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) H[3 * r + c] = E.h[r <= c ? hidx<6>(r, c) : hidx<6>(c, r)];
+                    atomic_block(T.val, eb[a * S + a], H);
+                }
                 atomic_force(force, iv[a], E.g[0], E.g[1], E.g[2]);
             }
             if (diag_b) {
-                double H[9];
+                if (kHess) {
+                    double H[9];
 #pragma unroll
-                for (int r = 0; r < 3; ++r)
+                    for (int r = 0; r < 3; ++r)
 #pragma unroll
-                    for (int c = 0; c < 3; ++c)
-                        H[3 * r + c] = E.h[r <= c ? hidx<6>(3 + r, 3 + c) : hidx<6>(3 + c, 3 + r)];
-                atomic_block(T.val, eb[b * S + b], H);
+                        for (int c = 0; c < 3; ++c)
+                            H[3 * r + c] = E.h[r <= c ? hidx<6>(3 + r, 3 + c) : hidx<6>(3 + c, 3 + r)];
+                    atomic_block(T.val, eb[b * S + b], H);
+                }
                 atomic_force(force, iv[b], E.g[3], E.g[4], E.g[5]);
             }
         }
 }
 
-__global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T, const float4 *__restrict__ pos,
+template <bool kHess>
+__global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T, const double *__restrict__ x,
                                                                 double *force, int n_elem)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -156,58 +179,38 @@ __global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T
             atomic_force(force, v, -prm[0] * prm[1], -prm[0] * prm[2], -prm[0] * prm[3]);
             return;
         }
-        // Anchor: 1/2 k |x - a|^2 on the anchor-relative position.
-        const float4 b = pos[2 * v], d = pos[2 * v + 1];
-        const double xa[3] = {(double(b.x) - prm[0]) + d.x, (double(b.y) - prm[1]) + d.y, (double(b.z) - prm[2]) + d.z};
+        // Anchor: 1/2 k |x - a|^2.
+        const double *xv = x + 3 * size_t(v);
         const double k = prm[3];
-        atomic_force(force, v, k * xa[0], k * xa[1], k * xa[2]);
-        const double H[9] = {k, 0.0, 0.0, 0.0, k, 0.0, 0.0, 0.0, k};
-        atomic_block(T.val, T.eblk[size_t(e) * 16], H);
+        atomic_force(force, v, k * (xv[0] - prm[0]), k * (xv[1] - prm[1]), k * (xv[2] - prm[2]));
+        if (kHess) {
+            const double H[9] = {k, 0.0, 0.0, 0.0, k, 0.0, 0.0, 0.0, k};
+            atomic_block(T.val, T.eblk[size_t(e) * 16], H);
+        }
         return;
     }
-    case 2: assemble_element<2>(T, pos, force, e, ix, info); break;
-    case 3: assemble_element<3>(T, pos, force, e, ix, info); break;
-    default: assemble_element<4>(T, pos, force, e, ix, info); break;
+    case 2: assemble_element<2, kHess>(T, x, force, e, ix, info); break;
+    case 3: assemble_element<3, kHess>(T, x, force, e, ix, info); break;
+    default: assemble_element<4, kHess>(T, x, force, e, ix, info); break;
     }
 }
 
-// x0 = x (rebased: base = fl(x), dold = the exact remainder), y = x + h v as the delta, and the
-// forces initialised to M g.
-__global__ void implicit_predict_kernel(float4 *pos, float4 *dold, const float4 *vel, const float *mass, double *force,
-                                       int nv, float h, double gx, double gy, double gz)
+// The system matrix alpha M + beta H (H = hess E = -K, assembled into val) and the diagonal
+// preconditioner 1 / A_ii (Eigen's DiagonalPreconditioner: 1 where A_ii is 0). One thread per
+// block row.
+__global__ void implicit_lhs_kernel(ImplicitTables T, const double *mass, int nv, double alpha, double beta,
+                                    double *dinv)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
-    const float4 b = pos[2 * i], d = pos[2 * i + 1];
-    const float4 v = vel[i];
-    float s[3], r[3];
-    const float bb[3] = {b.x, b.y, b.z}, dd[3] = {d.x, d.y, d.z};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        s[k] = bb[k] + dd[k];
-        const float t = s[k] - bb[k];
-        r[k] = (bb[k] - (s[k] - t)) + (dd[k] - t);
-    }
-    pos[2 * i] = make_float4(s[0], s[1], s[2], b.w);
-    pos[2 * i + 1] = make_float4(r[0] + h * v.x, r[1] + h * v.y, r[2] + h * v.z, 0.f);
-    dold[i] = make_float4(r[0], r[1], r[2], 0.f);
-    const double m = mass[i];
-    force[3 * i] = m * gx;
-    force[3 * i + 1] = m * gy;
-    force[3 * i + 2] = m * gz;
-}
-
-// The mass term M / h^2 on the diagonal blocks and the diagonal preconditioner 1 / A_ii.
-__global__ void implicit_mass_kernel(ImplicitTables T, const float *mass, int nv, double invh2, double *dinv)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nv) return;
+    if (beta != 1.0)
+        for (int k = T.row_ptr[i]; k < T.row_ptr[i + 1]; ++k)
+            for (int q = 0; q < 9; ++q) T.val[size_t(k) * 9 + q] *= beta;
     double *b = T.val + size_t(T.diag[i]) * 9;
-    const double m = double(mass[i]) * invh2;
+    const double m = alpha * mass[i];
     b[0] += m;
     b[4] += m;
     b[8] += m;
-    // Eigen's DiagonalPreconditioner: 1 / A_ii, or 1 where A_ii is 0.
     dinv[3 * i] = b[0] != 0.0 ? 1.0 / b[0] : 1.0;
     dinv[3 * i + 1] = b[4] != 0.0 ? 1.0 / b[4] : 1.0;
     dinv[3 * i + 2] = b[8] != 0.0 ? 1.0 / b[8] : 1.0;
@@ -227,7 +230,7 @@ __device__ __forceinline__ void block_reduce_add(double v, double *out)
     }
 }
 
-// Ap = A p (one thread per block row) and dots[0] += p . Ap.
+// Ap = A p (one thread per block row); with dots, dots[0] += p . Ap.
 __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -246,7 +249,7 @@ __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict_
         Ap[3 * i + 2] = y2;
         pap = p[3 * i] * y0 + p[3 * i + 1] * y1 + p[3 * i + 2] * y2;
     }
-    block_reduce_add(pap, dots);
+    if (dots) block_reduce_add(pap, dots);
 }
 
 // CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z (per component).
@@ -297,16 +300,117 @@ __global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, 
     p[i] = z[i] + beta * p[i];
 }
 
-// x = y + dx (the delta holds y).
-__global__ void implicit_apply_kernel(float4 *pos, const double *dx, int nv)
+// ---- vector steps of the methods (n = 3 V degrees of freedom; mass per vertex) ------------
+
+// f = M g (getSystemForce's gravity term), or 0.
+__global__ void force_init_kernel(double *f, const double *mass, int n, double gx, double gy, double gz, bool gravity)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nv) return;
-    float4 d = pos[2 * i + 1];
-    d.x = static_cast<float>(d.x + dx[3 * i]);
-    d.y = static_cast<float>(d.y + dx[3 * i + 1]);
-    d.z = static_cast<float>(d.z + dx[3 * i + 2]);
-    pos[2 * i + 1] = d;
+    if (i >= n) return;
+    const double g = i % 3 == 0 ? gx : (i % 3 == 1 ? gy : gz);
+    f[i] = gravity ? g * mass[i / 3] : 0.0;
+}
+
+// y = y + x s (integrateVelocities with x = v, s = h; updatePositionsFromDx with s = 1).
+__global__ void axpy_kernel(double *y, const double *x, double s, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = y[i] + x[i] * s;
+}
+
+// out = a + b s.
+__global__ void lincomb_kernel(double *out, const double *a, const double *b, double s, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = a[i] + b[i] * s;
+}
+
+// out = (a - b) s (computeIntegratedVelocities).
+__global__ void diffscale_kernel(double *out, const double *a, const double *b, double s, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (a[i] - b[i]) * s;
+}
+
+// out = s a.
+__global__ void scale_kernel(double *out, const double *a, double s, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = s * a[i];
+}
+
+// Baraff-Witkin: b = h (f + h (K v0)), K v0 = -u with u = H v0.
+__global__ void bw_rhs_kernel(double *b, const double *f, const double *u, double h, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = h * (f[i] + h * -u[i]);
+}
+
+// BDF2: w = x0 - x_-1 + 2 h v0.
+__global__ void bdf2_w_kernel(double *w, const double *x0, const double *xm1, const double *v0, double h2, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w[i] = (x0[i] - xm1[i]) + h2 * v0[i];
+}
+
+// BDF2: b = 1/3 M (v0 - v_-1) + 2/3 h (f + 1/3 K w), K w = -u with u = H w.
+__global__ void bdf2_rhs_kernel(double *b, const double *mass, const double *v0, const double *vm1, const double *f,
+                                const double *u, double h, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    b[i] = (1.0 / 3.0 * mass[i / 3]) * (v0[i] - vm1[i]) + (2.0 / 3.0 * h) * (f[i] + 1.0 / 3.0 * -u[i]);
+}
+
+// BDF2: x = 4/3 x0 - 1/3 x_-1 + 2/3 v h; then x_-1 = x0, v_-1 = v0.
+__global__ void bdf2_update_kernel(double *x, double *xm1, double *vm1, const double *x0, const double *v0,
+                                   const double *v, double h, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = (4.0 / 3.0 * x0[i] - 1.0 / 3.0 * xm1[i]) + 2.0 / 3.0 * v[i] * h;
+    xm1[i] = x0[i];
+    vm1[i] = v0[i];
+}
+
+// NewtonRobust: r = h f - M (v - v0); b = r when given; norm2 += |r|^2.
+__global__ void robust_rhs_kernel(double *b, const double *f, const double *v, const double *v0, const double *mass,
+                                  double h, int n, double *norm2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s = 0.0;
+    if (i < n) {
+        const double r = h * f[i] - mass[i / 3] * (v[i] - v0[i]);
+        if (b) b[i] = r;
+        s = r * r;
+    }
+    block_reduce_add(s, norm2);
+}
+
+// QuasiStaticNewtonRobust: r = f - (M / h) v; b = r when given; norm2 += |r|^2.
+__global__ void qs_rhs_kernel(double *b, const double *f, const double *v, const double *mass, double invdt, int n,
+                              double *norm2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s = 0.0;
+    if (i < n) {
+        const double r = f[i] - (invdt * mass[i / 3]) * v[i];
+        if (b) b[i] = r;
+        s = r * r;
+    }
+    block_reduce_add(s, norm2);
+}
+
+// SimplecticEuler: v += h g, then v += h W f_internal (W: inverse masses, 0 for massless).
+__global__ void symplectic_kernel(double *v, const double *f, const double *mass, double h, double dgx, double dgy,
+                                  double dgz, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double dg = i % 3 == 0 ? dgx : (i % 3 == 1 ? dgy : dgz);
+    const double m = mass[i / 3];
+    const double w = m == 0.0 ? 0.0 : 1.0 / m;
+    v[i] = (v[i] + dg) + w * f[i] * h;
 }
 
 static int grid_of(int n, int t = 256) { return (n + t - 1) / t; }
@@ -317,12 +421,17 @@ struct ImplicitSolver {
     int device{0};
     cudaStream_t stream{nullptr};
     cudaEvent_t ev0{nullptr}, ev1{nullptr};
-    ParticleState X;
     DevBuf d_idx, d_info, d_prm, d_eblk, d_row, d_col, d_val, d_diag, d_mass;
-    DevBuf d_force, d_dinv, d_x, d_r, d_z, d_p, d_Ap, d_dots;
+    DevBuf d_x, d_v, d_x0, d_v0, d_vi, d_xm1, d_vm1, d_f, d_b, d_u, d_w;
+    DevBuf d_dx, d_r, d_z, d_p, d_Ap, d_dinv, d_dots;
     HostBuf h_dots;
     ImplicitTables T{};
     int n_elem{0}, nnzb{0};
+    // Step control of the robust methods (m_currentDt, m_consecutiveSuccessfulSteps) and the
+    // BDF2 history (m_xMinusOne / m_vMinusOne initialised).
+    double current_dt{-1.0};
+    int successes{0};
+    bool history{false};
 
     ~ImplicitSolver()
     {
@@ -336,12 +445,16 @@ struct ImplicitSolver {
 
     static spgx_status check_params(const spgx_implicit_params *p)
     {
-        if (!p || !(p->dt > 0) || p->substeps < 1 || !(p->cg_threshold >= 0) || p->cg_max_iterations < 0) {
-            set_error("invalid implicit Euler parameters");
+        if (!p || !(p->dt > 0) || p->substeps < 1 || !(p->cg_threshold >= 0) || p->cg_max_iterations < 0 ||
+            p->method < SPGX_IMPLICIT_NEWTON_DX || p->method > SPGX_SYMPLECTIC_EULER) {
+            set_error("invalid implicit solver parameters");
             return SPGX_ERR_INVALID_ARG;
         }
         return SPGX_OK;
     }
+
+    int n3() const { return 3 * L.nv; }
+    double *vec(DevBuf &b) { return b.as<double>(); }
 
     spgx_status init(const spgx_scene_desc *scene, const spgx_implicit_params *params)
     {
@@ -358,16 +471,17 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         SPGX_CUDA(cudaEventCreate(&ev0));
         SPGX_CUDA(cudaEventCreate(&ev1));
-        SPGX_TRY_STATUS(X.init(L));
-        // Element list over every energy (internal vertex ids) and the block pattern.
+        // Element list over every energy (internal vertex ids), the block pattern and the FP64
+        // masses in internal order.
         const int nv = L.nv;
         std::vector<I4> idx, info;
-        std::vector<double> prm;
+        std::vector<double> prm, mass(std::max(1, nv), 0.0);
         std::vector<std::vector<int32_t>> nb(nv);
         for (int v = 0; v < nv; ++v) nb[v].push_back(v);
         for (int o = 0; o < scene->n_objects; ++o) {
             const auto &ob = scene->objects[o];
             const int vb = L.objects[o].vertex_base;
+            for (int k = 0; k < ob.n_vertices; ++k) mass[L.ext2int[vb + k]] = ob.mass[k];
             for (int e = 0; e < ob.n_energies; ++e) {
                 const auto &E = ob.energies[e];
                 const int S = stencil_size(E.type), Pc = param_count(E.type);
@@ -419,29 +533,68 @@ struct ImplicitSolver {
         SPGX_TRY_STATUS(d_row.upload(row));
         SPGX_TRY_STATUS(d_col.upload(col));
         SPGX_TRY_STATUS(d_diag.upload(diag.empty() ? std::vector<int32_t>{0} : diag));
-        SPGX_TRY_STATUS(d_mass.upload(L.mass.empty() ? std::vector<float>{0.f} : L.mass));
+        SPGX_TRY_STATUS(d_mass.upload(mass));
         SPGX_TRY_STATUS(d_val.alloc(size_t(std::max(1, nnzb)) * 9 * sizeof(double)));
-        const size_t vec = size_t(std::max(1, nv)) * 3 * sizeof(double);
-        for (DevBuf *b : {&d_force, &d_dinv, &d_x, &d_r, &d_z, &d_p, &d_Ap}) SPGX_TRY_STATUS(b->alloc(vec));
-        SPGX_TRY_STATUS(d_dots.alloc(size_t(2) * 3 * sizeof(double)));
-        SPGX_TRY_STATUS(h_dots.alloc(size_t(2) * 3 * sizeof(double)));
+        const size_t vb = size_t(std::max(1, nv)) * 3 * sizeof(double);
+        for (DevBuf *b : {&d_x, &d_v, &d_x0, &d_v0, &d_vi, &d_xm1, &d_vm1, &d_f, &d_b, &d_u, &d_w, &d_dx, &d_r, &d_z,
+                          &d_p, &d_Ap, &d_dinv})
+            SPGX_TRY_STATUS(b->alloc(vb));
+        SPGX_TRY_STATUS(d_dots.alloc(size_t(8) * sizeof(double)));
+        SPGX_TRY_STATUS(h_dots.alloc(size_t(8) * sizeof(double)));
         T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
                            d_col.as<int>(), d_val.as<double>(), d_diag.as<int>()};
+        std::vector<double> x(3 * size_t(std::max(1, nv)), 0.0), v(x.size(), 0.0);
+        for (int i = 0; i < nv; ++i) {
+            const int k = L.ext2int[i];
+            for (int a = 0; a < 3; ++a) {
+                x[3 * size_t(k) + a] = L.x_ext[3 * size_t(i) + a];
+                v[3 * size_t(k) + a] = L.v_ext[3 * size_t(i) + a];
+            }
+        }
+        SPGX_CUDA(cudaMemcpy(vec(d_x), x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice));
+        SPGX_CUDA(cudaMemcpy(vec(d_v), v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
         return SPGX_OK;
     }
 
-    // One CG solve of A dx = f (ImplicitEulerBase::solveLinearSystem, implicitEulerBase.cpp:227-239)
-    // with Eigen::ConjugateGradient's stopping rule |r|^2 < tol^2 |b|^2.
-    spgx_status cg(int &iterations, double &rel_residual)
+    // getSystemForce at x into d_f (gravity included unless told otherwise) and, with hessian,
+    // getSystemStiffnessMatrix as H = -K into the BSR values.
+    void assemble(const double *x, bool hessian, bool gravity = true)
     {
-        const int nv = L.nv;
+        const int n = n3();
+        force_init_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_f), vec(d_mass), n, P.gravity[0], P.gravity[1],
+                                                          P.gravity[2], gravity);
+        if (hessian) cudaMemsetAsync(d_val.as<double>(), 0, size_t(std::max(1, nnzb)) * 9 * sizeof(double), stream);
+        if (n_elem > 0) {
+            if (hessian)
+                implicit_assemble_kernel<true><<<grid_of(n_elem, 128), 128, 0, stream>>>(T, x, vec(d_f), n_elem);
+            else
+                implicit_assemble_kernel<false><<<grid_of(n_elem, 128), 128, 0, stream>>>(T, x, vec(d_f), n_elem);
+        }
+    }
+
+    // Reads the scalar accumulated at d_dots[7] (after the stream's work) and clears it.
+    spgx_status take_norm(double &out)
+    {
+        double *hd = h_dots.as<double>();
+        SPGX_CUDA(cudaMemcpyAsync(hd + 7, d_dots.as<double>() + 7, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaMemsetAsync(d_dots.as<double>() + 7, 0, sizeof(double), stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        out = std::sqrt(hd[7]);
+        return SPGX_OK;
+    }
+
+    // One CG solve of (alpha M + beta H) d_dx = d_b (ImplicitEulerBase::solveLinearSystem,
+    // implicitEulerBase.cpp:227-239) with Eigen::ConjugateGradient's stopping rule
+    // |r|^2 < tol^2 |b|^2. The BSR holds H on entry.
+    spgx_status cg(double alpha, double beta, int &iterations, double &rel_residual)
+    {
+        const int nv = L.nv, n = n3();
+        implicit_lhs_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_mass), nv, alpha, beta, vec(d_dinv));
         double *dots = d_dots.as<double>();  // two sets of {pAp, rr, rz}: [0..2] previous, [3..5] current
         double *hd = h_dots.as<double>();
         SPGX_CUDA(cudaMemsetAsync(dots, 0, 6 * sizeof(double), stream));
-        const int n = 3 * nv;
-        implicit_cg_init_kernel<<<grid_of(n), 256, 0, stream>>>(d_force.as<double>(), d_dinv.as<double>(),
-                                                                d_x.as<double>(), d_r.as<double>(), d_z.as<double>(),
-                                                                d_p.as<double>(), n, dots);
+        implicit_cg_init_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_b), vec(d_dinv), vec(d_dx), vec(d_r), vec(d_z),
+                                                                vec(d_p), n, dots);
         SPGX_CUDA(cudaMemcpyAsync(hd, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
         SPGX_CUDA(cudaStreamSynchronize(stream));
         const double rhs2 = hd[1];
@@ -452,16 +605,12 @@ struct ImplicitSolver {
         double rr = rhs2;
         double *prev = dots, *cur = dots + 3;
         while (rr >= thr2 && iterations < P.cg_max_iterations) {
-            // prev = {pAp, rr, rz} of this iteration's start
             SPGX_CUDA(cudaMemsetAsync(prev, 0, sizeof(double), stream));
-            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, d_p.as<double>(), d_Ap.as<double>(), nv, prev);
+            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_p), vec(d_Ap), nv, prev);
             SPGX_CUDA(cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream));
-            implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(d_x.as<double>(), d_r.as<double>(),
-                                                                     d_z.as<double>(), d_p.as<double>(),
-                                                                     d_Ap.as<double>(), d_dinv.as<double>(), n, prev,
-                                                                     cur);
-            implicit_cg_direction_kernel<<<grid_of(n), 256, 0, stream>>>(d_p.as<double>(), d_z.as<double>(), n, prev,
-                                                                         cur);
+            implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
+                                                                     vec(d_Ap), vec(d_dinv), n, prev, cur);
+            implicit_cg_direction_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_p), vec(d_z), n, prev, cur);
             SPGX_CUDA(cudaMemcpyAsync(hd, cur, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
             SPGX_CUDA(cudaStreamSynchronize(stream));
             rr = hd[1];
@@ -472,42 +621,321 @@ struct ImplicitSolver {
         return SPGX_OK;
     }
 
+    struct Tally {
+        int cg_iterations = 0, newton_iterations = 0, failed = 0;
+        bool converged = true;
+        double first_residual = -1.0, last_residual = 0.0;
+    };
+
+    spgx_status solve(double alpha, double beta, Tally &t)
+    {
+        int its = 0;
+        double rel = 0.0;
+        SPGX_TRY_STATUS(cg(alpha, beta, its, rel));
+        t.cg_iterations += its;
+        t.last_residual = rel;
+        if (rel > P.cg_threshold) t.converged = false;
+        return SPGX_OK;
+    }
+
+    // One substep of a method without step control.
+    spgx_status substep(double h, Tally &t)
+    {
+        const int n = n3(), g = grid_of(n);
+        double *x = vec(d_x), *v = vec(d_v), *x0 = vec(d_x0), *v0 = vec(d_v0), *f = vec(d_f), *b = vec(d_b);
+        const size_t bytes = size_t(n) * sizeof(double);
+        switch (P.method) {
+        case SPGX_IMPLICIT_NEWTON_DX: {
+            SPGX_CUDA(cudaMemcpyAsync(x0, x, bytes, cudaMemcpyDeviceToDevice, stream));
+            axpy_kernel<<<g, 256, 0, stream>>>(x, v, h, n);
+            assemble(x, true);
+            SPGX_CUDA(cudaMemcpyAsync(b, f, bytes, cudaMemcpyDeviceToDevice, stream));
+            const double invdt = 1. / h;
+            SPGX_TRY_STATUS(solve(invdt * invdt, 1.0, t));
+            axpy_kernel<<<g, 256, 0, stream>>>(x, vec(d_dx), 1.0, n);
+            diffscale_kernel<<<g, 256, 0, stream>>>(v, x, x0, invdt, n);
+            break;
+        }
+        case SPGX_IMPLICIT_NEWTON_DV: {
+            SPGX_CUDA(cudaMemcpyAsync(x0, x, bytes, cudaMemcpyDeviceToDevice, stream));
+            SPGX_CUDA(cudaMemcpyAsync(v0, v, bytes, cudaMemcpyDeviceToDevice, stream));
+            axpy_kernel<<<g, 256, 0, stream>>>(x, v, h, n);
+            assemble(x, true);
+            scale_kernel<<<g, 256, 0, stream>>>(b, f, h, n);
+            SPGX_TRY_STATUS(solve(1.0, h * h, t));
+            lincomb_kernel<<<g, 256, 0, stream>>>(v, v0, vec(d_dx), 1.0, n);
+            lincomb_kernel<<<g, 256, 0, stream>>>(x, x0, v, h, n);
+            break;
+        }
+        case SPGX_IMPLICIT_BARAFF_WITKIN: {
+            SPGX_CUDA(cudaMemcpyAsync(v0, v, bytes, cudaMemcpyDeviceToDevice, stream));
+            assemble(x, true);
+            implicit_spmv_kernel<<<grid_of(L.nv), 256, 0, stream>>>(T, v0, vec(d_u), L.nv, nullptr);
+            bw_rhs_kernel<<<g, 256, 0, stream>>>(b, f, vec(d_u), h, n);
+            SPGX_TRY_STATUS(solve(1.0, h * h, t));
+            lincomb_kernel<<<g, 256, 0, stream>>>(v, v0, vec(d_dx), 1.0, n);
+            axpy_kernel<<<g, 256, 0, stream>>>(x, v, h, n);
+            break;
+        }
+        case SPGX_IMPLICIT_BDF2: {
+            SPGX_CUDA(cudaMemcpyAsync(x0, x, bytes, cudaMemcpyDeviceToDevice, stream));
+            SPGX_CUDA(cudaMemcpyAsync(v0, v, bytes, cudaMemcpyDeviceToDevice, stream));
+            if (!history) {
+                SPGX_CUDA(cudaMemcpyAsync(vec(d_xm1), x, bytes, cudaMemcpyDeviceToDevice, stream));
+                SPGX_CUDA(cudaMemcpyAsync(vec(d_vm1), v, bytes, cudaMemcpyDeviceToDevice, stream));
+                history = true;
+            }
+            assemble(x, true);
+            bdf2_w_kernel<<<g, 256, 0, stream>>>(vec(d_w), x0, vec(d_xm1), v0, 2 * h, n);
+            implicit_spmv_kernel<<<grid_of(L.nv), 256, 0, stream>>>(T, vec(d_w), vec(d_u), L.nv, nullptr);
+            bdf2_rhs_kernel<<<g, 256, 0, stream>>>(b, vec(d_mass), v0, vec(d_vm1), f, vec(d_u), h, n);
+            SPGX_TRY_STATUS(solve(1.0, 4.0 / 9.0 * (h * h), t));
+            lincomb_kernel<<<g, 256, 0, stream>>>(v, v0, vec(d_dx), 1.0, n);
+            bdf2_update_kernel<<<g, 256, 0, stream>>>(x, vec(d_xm1), vec(d_vm1), x0, v0, v, h, n);
+            break;
+        }
+        case SPGX_STATIC_NEWTON: {
+            assemble(x, true);
+            scale_kernel<<<g, 256, 0, stream>>>(b, f, -1.0, n);
+            SPGX_TRY_STATUS(solve(0.0, -1.0, t));
+            axpy_kernel<<<g, 256, 0, stream>>>(x, vec(d_dx), 1.0, n);
+            break;
+        }
+        case SPGX_QUASI_STATIC_NEWTON: {
+            assemble(x, true);
+            const double dtdt = h * h;
+            scale_kernel<<<g, 256, 0, stream>>>(b, f, dtdt, n);
+            SPGX_TRY_STATUS(solve(1.0, dtdt, t));
+            axpy_kernel<<<g, 256, 0, stream>>>(x, vec(d_dx), 1.0, n);
+            break;
+        }
+        case SPGX_SYMPLECTIC_EULER: {
+            assemble(x, false, false);
+            symplectic_kernel<<<g, 256, 0, stream>>>(v, f, vec(d_mass), h, h * P.gravity[0], h * P.gravity[1],
+                                                     h * P.gravity[2], n);
+            axpy_kernel<<<g, 256, 0, stream>>>(x, v, h, n);
+            break;
+        }
+        default: break;
+        }
+        SPGX_CUDA(cudaGetLastError());
+        return SPGX_OK;
+    }
+
+    double begin_controlled(double &max_dt)
+    {
+        max_dt = P.dt / P.substeps;
+        if (current_dt == -1. || current_dt > max_dt) current_dt = max_dt;
+        return current_dt;
+    }
+
+    void end_controlled(bool ok, double max_dt, Tally &t)
+    {
+        if (!ok) {
+            current_dt *= 0.75;
+            successes = 0;
+            ++t.failed;
+            t.converged = false;
+        } else {
+            ++successes;
+            if (successes > 5 && current_dt < max_dt) current_dt /= 0.75;
+        }
+    }
+
+    // ImplicitEulerNewtonRobust substep (implicitEulerNewtonRobust.cpp:33-126).
+    spgx_status newton_robust(Tally &t)
+    {
+        const double threshold = 1e-5;
+        const int n = n3(), g = grid_of(n);
+        const size_t bytes = size_t(n) * sizeof(double);
+        double *x = vec(d_x), *v = vec(d_v), *x0 = vec(d_x0), *v0 = vec(d_v0), *vi = vec(d_vi);
+        double *norm2 = d_dots.as<double>() + 7;
+        double max_dt;
+        const double dt = begin_controlled(max_dt);
+        bool ok = true;
+        SPGX_CUDA(cudaMemcpyAsync(x0, x, bytes, cudaMemcpyDeviceToDevice, stream));
+        SPGX_CUDA(cudaMemcpyAsync(v0, v, bytes, cudaMemcpyDeviceToDevice, stream));
+        SPGX_CUDA(cudaMemsetAsync(norm2, 0, sizeof(double), stream));
+        axpy_kernel<<<g, 256, 0, stream>>>(x, v, dt, n);
+        SPGX_CUDA(cudaMemcpyAsync(vi, v0, bytes, cudaMemcpyDeviceToDevice, stream));
+        int it = 0;
+        double res = 0.0;
+        do {
+            assemble(x, true);
+            robust_rhs_kernel<<<g, 256, 0, stream>>>(vec(d_b), vec(d_f), vi, v0, vec(d_mass), dt, n, norm2);
+            double r0;
+            SPGX_TRY_STATUS(take_norm(r0));
+            if (t.first_residual < 0) t.first_residual = r0;
+            SPGX_TRY_STATUS(solve(1.0, dt * dt, t));
+            res = r0;
+            int ls = 0;
+            double alpha = 1.;
+            while (res >= r0 && ls < 5) {
+                lincomb_kernel<<<g, 256, 0, stream>>>(v, vi, vec(d_dx), alpha, n);
+                lincomb_kernel<<<g, 256, 0, stream>>>(x, x0, v, dt, n);
+                assemble(x, false);
+                robust_rhs_kernel<<<g, 256, 0, stream>>>(nullptr, vec(d_f), v, v0, vec(d_mass), dt, n, norm2);
+                SPGX_TRY_STATUS(take_norm(res));
+                if (res < r0) SPGX_CUDA(cudaMemcpyAsync(vi, v, bytes, cudaMemcpyDeviceToDevice, stream));
+                alpha *= 0.5;
+                ++ls;
+            }
+            if (res >= r0 && res > threshold) ok = false;
+            ++it;
+        } while (res > threshold && ok && it < 5);
+        t.newton_iterations += it;
+        t.last_residual = res;
+        if (res > threshold) ok = false;
+        if (!ok) {
+            SPGX_CUDA(cudaMemcpyAsync(x, x0, bytes, cudaMemcpyDeviceToDevice, stream));
+            SPGX_CUDA(cudaMemcpyAsync(v, v0, bytes, cudaMemcpyDeviceToDevice, stream));
+        }
+        end_controlled(ok, max_dt, t);
+        SPGX_CUDA(cudaGetLastError());
+        return SPGX_OK;
+    }
+
+    // QuasiStaticNewtonRobust substep (quasiStaticNewtonRobust.cpp:33-136).
+    spgx_status quasi_static_robust(Tally &t)
+    {
+        const double threshold = 1e-2;
+        const int n = n3(), g = grid_of(n);
+        const size_t bytes = size_t(n) * sizeof(double);
+        double *x = vec(d_x), *v = vec(d_v), *x0 = vec(d_x0), *xi = vec(d_vi);
+        double *norm2 = d_dots.as<double>() + 7;
+        double max_dt;
+        const double dt = begin_controlled(max_dt);
+        const double invdt = 1 / dt;
+        const double invdt2 = invdt * invdt;
+        bool ok = true;
+        SPGX_CUDA(cudaMemcpyAsync(x0, x, bytes, cudaMemcpyDeviceToDevice, stream));
+        SPGX_CUDA(cudaMemcpyAsync(xi, x0, bytes, cudaMemcpyDeviceToDevice, stream));
+        SPGX_CUDA(cudaMemsetAsync(norm2, 0, sizeof(double), stream));
+        int it = 0;
+        double res = 0.0;
+        do {
+            assemble(x, true);
+            diffscale_kernel<<<g, 256, 0, stream>>>(v, x, x0, invdt, n);
+            qs_rhs_kernel<<<g, 256, 0, stream>>>(vec(d_b), vec(d_f), v, vec(d_mass), invdt, n, norm2);
+            double r0;
+            SPGX_TRY_STATUS(take_norm(r0));
+            if (t.first_residual < 0) t.first_residual = r0;
+            SPGX_TRY_STATUS(solve(invdt2, 1.0, t));
+            res = r0;
+            int ls = 0;
+            double alpha = 1.;
+            while (res >= r0 && ls < 5) {
+                lincomb_kernel<<<g, 256, 0, stream>>>(x, xi, vec(d_dx), alpha, n);
+                diffscale_kernel<<<g, 256, 0, stream>>>(v, x, x0, invdt, n);
+                assemble(x, false);
+                qs_rhs_kernel<<<g, 256, 0, stream>>>(nullptr, vec(d_f), v, vec(d_mass), invdt, n, norm2);
+                SPGX_TRY_STATUS(take_norm(res));
+                if (res < r0) SPGX_CUDA(cudaMemcpyAsync(xi, x, bytes, cudaMemcpyDeviceToDevice, stream));
+                alpha *= 0.5;
+                ++ls;
+            }
+            if (res >= r0 && res > threshold) ok = false;
+            ++it;
+        } while (res > threshold && ok && it < 5);
+        t.newton_iterations += it;
+        t.last_residual = res;
+        if (res > threshold) ok = false;
+        if (!ok) SPGX_CUDA(cudaMemcpyAsync(x, x0, bytes, cudaMemcpyDeviceToDevice, stream));
+        end_controlled(ok, max_dt, t);
+        SPGX_CUDA(cudaGetLastError());
+        return SPGX_OK;
+    }
+
     spgx_status step(spgx_step_stats *stats)
     {
-        SPGX_TRY_STATUS(X.upload_if_dirty(stream));
-        X.mark_device_advanced();
-        spgx_step_stats st{};
-        st.converged = 1;
+        Tally t;
         const int nv = L.nv;
         const double h = P.dt / P.substeps;
         SPGX_CUDA(cudaEventRecord(ev0, stream));
         for (int s = 0; s < P.substeps && nv > 0; ++s) {
-            implicit_predict_kernel<<<grid_of(nv), 256, 0, stream>>>(X.pos(), X.dold(), X.vel(), d_mass.as<float>(),
-                                                                     d_force.as<double>(), nv, float(h), P.gravity[0],
-                                                                     P.gravity[1], P.gravity[2]);
-            SPGX_CUDA(cudaMemsetAsync(d_val.as<double>(), 0, size_t(std::max(1, nnzb)) * 9 * sizeof(double), stream));
-            if (n_elem > 0)
-                implicit_assemble_kernel<<<grid_of(n_elem, 128), 128, 0, stream>>>(T, X.pos(), d_force.as<double>(),
-                                                                                  n_elem);
-            implicit_mass_kernel<<<grid_of(nv), 256, 0, stream>>>(T, d_mass.as<float>(), nv, 1.0 / (h * h),
-                                                                  d_dinv.as<double>());
-            SPGX_CUDA(cudaGetLastError());
-            int its = 0;
-            double rel = 0.0;
-            SPGX_TRY_STATUS(cg(its, rel));
-            st.iterations += its;
-            st.residual_final = rel;
-            if (rel > P.cg_threshold) st.converged = 0;
-            implicit_apply_kernel<<<grid_of(nv), 256, 0, stream>>>(X.pos(), d_x.as<double>(), nv);
-            launch_end_substep(X, h, stream);
+            if (P.method == SPGX_IMPLICIT_NEWTON_ROBUST)
+                SPGX_TRY_STATUS(newton_robust(t));
+            else if (P.method == SPGX_QUASI_STATIC_NEWTON_ROBUST)
+                SPGX_TRY_STATUS(quasi_static_robust(t));
+            else
+                SPGX_TRY_STATUS(substep(h, t));
         }
         SPGX_CUDA(cudaEventRecord(ev1, stream));
         SPGX_CUDA(cudaGetLastError());
         SPGX_CUDA(cudaStreamSynchronize(stream));
         float ms = 0.f;
         SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        spgx_step_stats st{};
+        st.iterations = t.cg_iterations;
+        st.fallback_solves = t.newton_iterations;
+        st.skipped_solves = t.failed;
+        st.converged = t.converged ? 1 : 0;
+        st.residual_initial = t.first_residual < 0 ? 0.0 : t.first_residual;
+        st.residual_final = t.last_residual;
         st.device_ms = ms;
         if (stats) *stats = st;
+        return SPGX_OK;
+    }
+
+    // State in the external order of one object.
+    spgx_status get(int obj, double *x, double *v)
+    {
+        if (obj < 0 || obj >= static_cast<int>(L.objects.size())) {
+            set_error("invalid object index");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        const size_t n = 3 * size_t(std::max(1, L.nv));
+        std::vector<double> hx(n), hv(n);
+        SPGX_CUDA(cudaMemcpyAsync(hx.data(), vec(d_x), n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaMemcpyAsync(hv.data(), vec(d_v), n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        const auto &O = L.objects[obj];
+        for (int k = 0; k < O.nv; ++k) {
+            const size_t i = size_t(L.ext2int[O.vertex_base + k]);
+            for (int a = 0; a < 3; ++a) {
+                if (x) x[3 * k + a] = hx[3 * i + a];
+                if (v) v[3 * k + a] = hv[3 * i + a];
+            }
+        }
+        return SPGX_OK;
+    }
+
+    spgx_status set(int obj, const double *x, const double *v)
+    {
+        if (obj < 0 || obj >= static_cast<int>(L.objects.size())) {
+            set_error("invalid object index");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        const size_t n = 3 * size_t(std::max(1, L.nv));
+        std::vector<double> hx(n), hv(n);
+        SPGX_CUDA(cudaMemcpyAsync(hx.data(), vec(d_x), n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaMemcpyAsync(hv.data(), vec(d_v), n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        const auto &O = L.objects[obj];
+        for (int k = 0; k < O.nv; ++k) {
+            const size_t i = size_t(L.ext2int[O.vertex_base + k]);
+            for (int a = 0; a < 3; ++a) {
+                if (x) hx[3 * i + a] = x[3 * k + a];
+                if (v) hv[3 * i + a] = v[3 * k + a];
+            }
+        }
+        SPGX_CUDA(cudaMemcpyAsync(vec(d_x), hx.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream));
+        SPGX_CUDA(cudaMemcpyAsync(vec(d_v), hv.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        return SPGX_OK;
+    }
+
+    // BaseSolver::reset: initial positions, zero velocities; the robust methods' step control
+    // and BDF2's history start over (NewtonRobust::reset, BDF2::reset).
+    spgx_status reset()
+    {
+        for (int o = 0; o < static_cast<int>(L.objects.size()); ++o) {
+            const std::vector<double> zeros(L.objects[o].x_init.size(), 0.0);
+            SPGX_TRY_STATUS(set(o, L.objects[o].x_init.data(), zeros.data()));
+        }
+        current_dt = -1.0;
+        successes = 0;
+        history = false;
         return SPGX_OK;
     }
 };
@@ -535,6 +963,7 @@ void spgx_implicit_params_default(spgx_implicit_params *p)
     p->cg_threshold = 1e-5;
     p->cg_max_iterations = 300;
     p->device = 0;
+    p->method = SPGX_IMPLICIT_NEWTON_DX;
 }
 
 spgx_status spgx_implicit_create(const spgx_scene_desc *scene, const spgx_implicit_params *params, spgx_implicit **out)
@@ -583,7 +1012,7 @@ spgx_status spgx_implicit_get_state(spgx_implicit *h, int32_t object, double *x,
 {
     SPGX_GUARD_BEGIN
     SPGX_IHANDLE(h);
-    return h->s->X.get(h->s->L, object, x, v, h->s->stream);
+    return h->s->get(object, x, v);
     SPGX_GUARD_END
 }
 
@@ -591,7 +1020,7 @@ spgx_status spgx_implicit_set_state(spgx_implicit *h, int32_t object, const doub
 {
     SPGX_GUARD_BEGIN
     SPGX_IHANDLE(h);
-    return h->s->X.set(h->s->L, object, x, v, h->s->stream);
+    return h->s->set(object, x, v);
     SPGX_GUARD_END
 }
 
@@ -599,7 +1028,20 @@ spgx_status spgx_implicit_reset(spgx_implicit *h)
 {
     SPGX_GUARD_BEGIN
     SPGX_IHANDLE(h);
-    return h->s->X.reset(h->s->L, h->s->stream);
+    return h->s->reset();
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_implicit_get_step_size(spgx_implicit *h, double *dt)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_IHANDLE(h);
+    if (!dt) {
+        spgx::set_error("dt is NULL");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    *dt = h->s->current_dt;
+    return SPGX_OK;
     SPGX_GUARD_END
 }
 

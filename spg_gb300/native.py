@@ -63,7 +63,8 @@ class XpbdParams(C.Structure):
 
 class ImplicitParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("substeps", C.c_int32), ("gravity", C.c_double * 3),
-                ("cg_threshold", C.c_double), ("cg_max_iterations", C.c_int32), ("device", C.c_int32)]
+                ("cg_threshold", C.c_double), ("cg_max_iterations", C.c_int32), ("device", C.c_int32),
+                ("method", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -146,6 +147,7 @@ def lib():
         L.spgx_implicit_get_state.argtypes = [vp, i32, dp, dp]
         L.spgx_implicit_set_state.argtypes = [vp, i32, dp, dp]
         L.spgx_implicit_reset.argtypes = [vp]
+        L.spgx_implicit_get_step_size.argtypes = [vp, dp]
         _lib = L
     return _lib
 
@@ -380,11 +382,17 @@ class Mlp:
         return loss.value
 
 
+(NEWTON_DX, NEWTON_DV, NEWTON_ROBUST, BARAFF_WITKIN, BDF2, STATIC_NEWTON, QUASI_STATIC_NEWTON,
+ QUASI_STATIC_NEWTON_ROBUST, SYMPLECTIC_EULER) = range(9)
+
+
 class ImplicitSolver:
-    """Implicit Euler with one Newton step per substep (ImplicitEulerNewtonDx) on one GPU."""
+    """The reference's global solvers on one GPU: `method` is one of NEWTON_DX (default),
+    NEWTON_DV, NEWTON_ROBUST, BARAFF_WITKIN, BDF2, STATIC_NEWTON, QUASI_STATIC_NEWTON,
+    QUASI_STATIC_NEWTON_ROBUST and SYMPLECTIC_EULER."""
 
     def __init__(self, objects, dt=0.01, substeps=1, gravity=(0.0, -9.8, 0.0), cg_threshold=1e-5,
-                 cg_max_iterations=300, device=0):
+                 cg_max_iterations=300, device=0, method=NEWTON_DX):
         self.objects_nv = [len(np.asarray(o.mass).reshape(-1)) for o in objects]
         self._d = Descriptor(objects)
         p = ImplicitParams()
@@ -392,6 +400,7 @@ class ImplicitSolver:
         p.dt, p.substeps = dt, substeps
         p.gravity = (C.c_double * 3)(*gravity)
         p.cg_threshold, p.cg_max_iterations, p.device = cg_threshold, cg_max_iterations, device
+        p.method = method
         self.params = p
         h = C.c_void_p()
         check(lib().spgx_implicit_create(C.byref(self._d.scene), C.byref(p), C.byref(h)))
@@ -423,6 +432,12 @@ class ImplicitSolver:
 
     def reset(self):
         check(lib().spgx_implicit_reset(self.h))
+
+    def step_size(self) -> float:
+        """The robust methods' current substep (-1 before the first step)."""
+        d = C.c_double()
+        check(lib().spgx_implicit_get_step_size(self.h, C.byref(d)))
+        return d.value
 
 
 class XpbdSolver:

@@ -65,3 +65,59 @@ def test_positions_after_10_steps_match_oracle(name):
     print(f"implicit {name}: max |dx| after 10 steps {err:.3g} m (extent {extent:.3g} m); CG iterations "
           f"GPU/oracle {its[:3]}")
     assert err <= 1e-4 * extent
+
+
+# ---------------------------------------------------------------------------------------
+# The other global solvers (NewtonDv, NewtonRobust, BaraffWitkin, BDF2, StaticNewton,
+# QuasiStaticNewton, QuasiStaticNewtonRobust, SimplecticEuler), each on scenes where the
+# FP64 oracle itself is well conditioned (a 1e-9 m perturbation of the start stays below
+# 1e-8 m after 10 steps). The robust methods also run on the StVK cloth, where their step
+# control rejects substeps and shrinks the step: the GPU must take the same decisions.
+
+def _method_cases():
+    cases = []
+    for m in (IR.NEWTON_DV, IR.BARAFF_WITKIN, IR.BDF2, IR.STATIC_NEWTON, IR.QUASI_STATIC_NEWTON):
+        cases += [(m, "snh_beam"), (m, "truss")]
+    for m in (IR.NEWTON_ROBUST, IR.QUASI_STATIC_NEWTON_ROBUST):
+        cases += [(m, "snh_beam"), (m, "stvk_cloth")]
+    cases += [(IR.SYMPLECTIC_EULER, "snh_beam"), (IR.SYMPLECTIC_EULER, "truss")]
+    return cases
+
+
+def test_oracle_methods_step():
+    obj = _scenes()["snh_beam"]
+    for m in range(9):
+        dt = 1e-4 if m == IR.SYMPLECTIC_EULER else 1 / 60
+        s = IR.ImplicitSolver(obj, dt, 1, scenes.GRAVITY, m)
+        s.step()
+        x, v = s.state()
+        assert np.all(np.isfinite(x)) and np.abs(x - obj.x).max() > 0, m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method,name", _method_cases())
+def test_methods_match_oracle(method, name):
+    N = pytest.importorskip("spg_gb300.native")
+    obj = _scenes()[name].copy()
+    dt = 1 / 60
+    if method == IR.SYMPLECTIC_EULER:
+        dt = 1e-4   # explicit: below the bar's stability limit; start stretched by 2 % along x
+        obj.x = obj.x0 + 0.02 * (obj.x0 - obj.x0.mean(0)) * np.array([1.0, 0.0, 0.0])
+    gpu = N.ImplicitSolver([obj], dt=dt, substeps=1, gravity=scenes.GRAVITY, method=method)
+    ref = IR.ImplicitSolver(obj, dt, 1, scenes.GRAVITY, method)
+    failed = 0
+    for _ in range(10):
+        st = gpu.step()
+        ref.step()
+        failed += int(st.skipped_solves)
+    xg, vg = gpu.state(0)
+    xr, vr = ref.state()
+    extent = float(np.ptp(obj.x0, axis=0).max())
+    err = float(np.abs(xg - xr).max())
+    moved = float(np.abs(xr - obj.x).max())
+    print(f"method {method} on {name}: max |dx| {err:.3g} m after 10 steps (moved {moved:.3g} m), "
+          f"failed substeps GPU/oracle {failed}/{ref.failed_substeps}")
+    assert err <= 1e-4 * extent and err <= 1e-3 * moved
+    if method in (IR.NEWTON_ROBUST, IR.QUASI_STATIC_NEWTON_ROBUST):
+        assert failed == ref.failed_substeps
+        assert gpu.step_size() == ref.current_dt
