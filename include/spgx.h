@@ -403,7 +403,7 @@ typedef struct spgx_implicit_params {
     double cg_threshold;       /* ImplicitEulerBase::m_cgThreshold (1e-5) */
     int32_t cg_max_iterations; /* ImplicitEulerBase::m_cgMaxIterations (300) */
     int32_t device;
-    int32_t method;            /* spgx_implicit_method (default NEWTON_DX) */
+    int32_t method;            /* an spgx_implicit_method value; default NEWTON_DX */
 } spgx_implicit_params;
 
 void spgx_implicit_params_default(spgx_implicit_params *p);
