@@ -1,6 +1,7 @@
 // Particle state management and the substep kernels shared by VBD and XPBD.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "api_internal.h"
@@ -83,6 +84,43 @@ void launch_end_substep(const ParticleState &P, double h, cudaStream_t st, float
     end_substep_kernel<<<(P.nv + 255) / 256, 256, 0, st>>>(P.pos(), P.dold(), P.vel(), P.nv, float(1.0 / h));
 }
 
+// One object's FP64 external-order state -> the device layout (base = fl(x), delta =
+// fl(x - base), velocity rounded to FP32); a NULL array leaves that part unchanged.
+__global__ void state_set_kernel(float4 *pos, float4 *vel, const int *ext2int, const double *x, const double *v,
+                                 int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = ext2int[k];
+    if (x) {
+        const double px = x[3 * k], py = x[3 * k + 1], pz = x[3 * k + 2];
+        const float bx = float(px), by = float(py), bz = float(pz);
+        pos[2 * i] = make_float4(bx, by, bz, 0.f);
+        pos[2 * i + 1] = make_float4(float(px - bx), float(py - by), float(pz - bz), 0.f);
+    }
+    if (v) vel[i] = make_float4(float(v[3 * k]), float(v[3 * k + 1]), float(v[3 * k + 2]), 0.f);
+}
+
+// The device layout -> one object's FP64 external-order state (x = base + delta).
+__global__ void state_get_kernel(const float4 *pos, const float4 *vel, const int *ext2int, double *x, double *v, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = ext2int[k];
+    if (x) {
+        const float4 b = pos[2 * i], d = pos[2 * i + 1];
+        x[3 * k] = double(b.x) + double(d.x);
+        x[3 * k + 1] = double(b.y) + double(d.y);
+        x[3 * k + 2] = double(b.z) + double(d.z);
+    }
+    if (v) {
+        const float4 u = vel[i];
+        v[3 * k] = u.x;
+        v[3 * k + 1] = u.y;
+        v[3 * k + 2] = u.z;
+    }
+}
+
 spgx_status ParticleState::init(const SceneLayout &L)
 {
     nv = L.nv;
@@ -91,12 +129,13 @@ spgx_status ParticleState::init(const SceneLayout &L)
     SPGX_TRY_STATUS(d_tgt.alloc(n * sizeof(float4)));
     SPGX_TRY_STATUS(d_dold.alloc(n * sizeof(float4)));
     SPGX_TRY_STATUS(d_vel.alloc(n * sizeof(float4)));
-    SPGX_TRY_STATUS(h_pos.alloc(n * 2 * sizeof(float4)));
-    SPGX_TRY_STATUS(h_vel.alloc(n * sizeof(float4)));
-    std::vector<float4> tg(n);
+    size_t max_obj = 1;
+    for (const auto &o : L.objects) max_obj = std::max(max_obj, size_t(o.nv));
+    stage_doubles = 6 * max_obj;
+    SPGX_TRY_STATUS(d_stage.alloc(stage_doubles * sizeof(double)));
+    SPGX_TRY_STATUS(d_ext2int.upload(L.ext2int.empty() ? std::vector<int32_t>{0} : L.ext2int));
+    std::vector<float4> hp(2 * n), hv(n), tg(n);
     std::vector<float> invm(n);
-    float4 *hp = h_pos.as<float4>();
-    float4 *hv = h_vel.as<float4>();
     for (size_t ext = 0; ext < n; ++ext) {
         const int i = L.ext2int[ext];
         const double *x = &L.x_ext[3 * ext];
@@ -109,34 +148,13 @@ spgx_status ParticleState::init(const SceneLayout &L)
         // ParticleGroup::addParticle: w = (m == 0 ? 0 : 1 / m), particleGroup.cpp:81
         invm[i] = L.mass[i] == 0.f ? 0.f : 1.f / L.mass[i];
     }
-    SPGX_CUDA(cudaMemcpy(pos(), hp, n * 2 * sizeof(float4), cudaMemcpyHostToDevice));
-    SPGX_CUDA(cudaMemcpy(vel(), hv, n * sizeof(float4), cudaMemcpyHostToDevice));
-    SPGX_CUDA(cudaMemcpy(tgt(), tg.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-    SPGX_CUDA(cudaMemset(dold(), 0, n * sizeof(float4)));
+    if (n) {
+        SPGX_CUDA(cudaMemcpy(pos(), hp.data(), n * 2 * sizeof(float4), cudaMemcpyHostToDevice));
+        SPGX_CUDA(cudaMemcpy(vel(), hv.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        SPGX_CUDA(cudaMemcpy(tgt(), tg.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+        SPGX_CUDA(cudaMemset(dold(), 0, n * sizeof(float4)));
+    }
     SPGX_TRY_STATUS(d_invm.upload(invm));
-    host_valid = true;
-    device_dirty = false;
-    return SPGX_OK;
-}
-
-spgx_status ParticleState::upload_if_dirty(cudaStream_t stream)
-{
-    if (!device_dirty) return SPGX_OK;
-    const size_t n = size_t(nv);
-    SPGX_CUDA(cudaMemcpyAsync(pos(), h_pos.as<void>(), n * 2 * sizeof(float4), cudaMemcpyHostToDevice, stream));
-    SPGX_CUDA(cudaMemcpyAsync(vel(), h_vel.as<void>(), n * sizeof(float4), cudaMemcpyHostToDevice, stream));
-    device_dirty = false;
-    return SPGX_OK;
-}
-
-spgx_status ParticleState::download_if_stale(cudaStream_t stream)
-{
-    if (host_valid) return SPGX_OK;
-    const size_t n = size_t(nv);
-    SPGX_CUDA(cudaMemcpyAsync(h_pos.as<void>(), pos(), n * 2 * sizeof(float4), cudaMemcpyDeviceToHost, stream));
-    SPGX_CUDA(cudaMemcpyAsync(h_vel.as<void>(), vel(), n * sizeof(float4), cudaMemcpyDeviceToHost, stream));
-    SPGX_CUDA(cudaStreamSynchronize(stream));
-    host_valid = true;
     return SPGX_OK;
 }
 
@@ -146,23 +164,16 @@ spgx_status ParticleState::get(const SceneLayout &L, int obj, double *x, double 
         set_error("invalid object index");
         return SPGX_ERR_INVALID_ARG;
     }
-    SPGX_TRY_STATUS(download_if_stale(stream));
     const auto &O = L.objects[obj];
-    const float4 *hp = h_pos.as<float4>();
-    const float4 *hv = h_vel.as<float4>();
-    for (int k = 0; k < O.nv; ++k) {
-        const int i = L.ext2int[O.vertex_base + k];
-        if (x) {
-            x[3 * k + 0] = double(hp[2 * i].x) + double(hp[2 * i + 1].x);
-            x[3 * k + 1] = double(hp[2 * i].y) + double(hp[2 * i + 1].y);
-            x[3 * k + 2] = double(hp[2 * i].z) + double(hp[2 * i + 1].z);
-        }
-        if (v) {
-            v[3 * k + 0] = hv[i].x;
-            v[3 * k + 1] = hv[i].y;
-            v[3 * k + 2] = hv[i].z;
-        }
-    }
+    const size_t n = size_t(O.nv);
+    if (n == 0 || (!x && !v)) return SPGX_OK;
+    double *sx = d_stage.as<double>(), *sv = sx + 3 * n;
+    state_get_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(pos(), vel(), d_ext2int.as<int>() + O.vertex_base,
+                                                                     x ? sx : nullptr, v ? sv : nullptr, int(n));
+    SPGX_CUDA(cudaGetLastError());
+    if (x) SPGX_CUDA(cudaMemcpyAsync(x, sx, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    if (v) SPGX_CUDA(cudaMemcpyAsync(v, sv, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    SPGX_CUDA(cudaStreamSynchronize(stream));
     return SPGX_OK;
 }
 
@@ -172,21 +183,19 @@ spgx_status ParticleState::set(const SceneLayout &L, int obj, const double *x, c
         set_error("invalid object index");
         return SPGX_ERR_INVALID_ARG;
     }
-    SPGX_TRY_STATUS(download_if_stale(stream));
     const auto &O = L.objects[obj];
-    float4 *hp = h_pos.as<float4>();
-    float4 *hv = h_vel.as<float4>();
-    for (int k = 0; k < O.nv; ++k) {
-        const int i = L.ext2int[O.vertex_base + k];
-        if (x) {
-            const float bx = float(x[3 * k]), by = float(x[3 * k + 1]), bz = float(x[3 * k + 2]);
-            hp[2 * i] = make_float4(bx, by, bz, 0.f);
-            hp[2 * i + 1] =
-                make_float4(float(x[3 * k] - bx), float(x[3 * k + 1] - by), float(x[3 * k + 2] - bz), 0.f);
-        }
-        if (v) hv[i] = make_float4(float(v[3 * k]), float(v[3 * k + 1]), float(v[3 * k + 2]), 0.f);
-    }
-    device_dirty = true;
+    const size_t n = size_t(O.nv);
+    if (n == 0 || (!x && !v)) return SPGX_OK;
+    double *sx = d_stage.as<double>(), *sv = sx + 3 * n;
+    if (x) SPGX_CUDA(cudaMemcpyAsync(sx, x, 3 * n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    if (v) SPGX_CUDA(cudaMemcpyAsync(sv, v, 3 * n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    state_set_kernel<<<unsigned((n + 255) / 256), 256, 0, stream>>>(pos(), vel(), d_ext2int.as<int>() + O.vertex_base,
+                                                                     x ? sx : nullptr, v ? sv : nullptr, int(n));
+    SPGX_CUDA(cudaGetLastError());
+    // The staging buffer is reused by the next call: the copies must have left the caller's
+    // arrays before returning (pageable sources are copied synchronously anyway).
+    SPGX_CUDA(cudaStreamSynchronize(stream));
+    replaced = true;
     return SPGX_OK;
 }
 

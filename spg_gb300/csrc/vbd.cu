@@ -1058,8 +1058,7 @@ void VbdSolver::launch_warm(cudaStream_t st)
 // history at constant velocity.
 spgx_status VbdSolver::upload_state()
 {
-    const bool replaced = X.device_dirty;
-    SPGX_TRY_STATUS(X.upload_if_dirty(stream));
+    const bool replaced = X.take_replaced();
     if (replaced && W.history)
         SPGX_CUDA(cudaMemcpyAsync(W.vhist.as<void>(), X.vel(), size_t(L.nv) * sizeof(float4),
                                   cudaMemcpyDeviceToDevice, stream));
