@@ -169,13 +169,16 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     const int lane = threadIdx.x & (G - 1);
     int *sidx = reinterpret_cast<int *>(srec + V.max_records);
 
-    // Static data of a task: its header, the indices of its local vertices (into sidx, async)
-    // and the header and record offset of the thread's vertex.
-    auto fetch_static = [&](int task, int4 &h0, int4 &h1, int4 &hv, int &roff) {
+    // Static data of a task, fetched while the previous task finishes or its dependencies are
+    // polled: its header, its record block and the indices of its local vertices (both into
+    // shared memory, async), and the header, record offset and inertial target of the thread's
+    // vertex. The target y is fixed for the whole step.
+    auto fetch_static = [&](int task, int4 &h0, int4 &h1, int4 &hv, int &roff, float4 &tg) {
         const int tile = task % n_tiles;
         h0 = __ldg(V.hdr + 2 * tile);
         h1 = __ldg(V.hdr + 2 * tile + 1);
         const int nvt = h0.y, nl = h0.y + h0.w;
+        for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
         for (int i = threadIdx.x; i < nl; i += blockDim.x) {
             if (i < nvt)
                 sidx[i] = h0.x + i;
@@ -184,9 +187,11 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         }
         hv = make_int4(0, 0, 0, 0);
         roff = 0;
+        tg = make_float4(0.f, 0.f, 0.f, 0.f);
         if (lv < nvt) {
             hv = __ldg(S.hdr + h0.x + lv);
             roff = __ldg(V.vrec + h0.x + lv);
+            tg = S.tgt[h0.x + lv];
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
@@ -196,7 +201,8 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     int task = s_next;
     int4 h0, h1, hv;
     int roff;
-    if (task < total) fetch_static(task, h0, h1, hv, roff);
+    float4 tg;
+    if (task < total) fetch_static(task, h0, h1, hv, roff, tg);
     while (task < total) {
         const int k = task / n_tiles;
         const int tile = task - k * n_tiles;
@@ -220,8 +226,8 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             ok = __all_sync(0xffffffffu, ok);
             if (threadIdx.x == 0) s_fail = !ok;
         }
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // this thread's index copies
-        __syncthreads();  // every thread's index copies, and the poll result
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // this thread's index and record copies
+        __syncthreads();  // every thread's index and record copies, and the poll result
         if (s_fail) {
             if (threadIdx.x == 0) {
                 atomicExch(F.ticket + 1, 1);
@@ -229,8 +235,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             }
             break;
         }
-        // Stage the records and the current positions of the local vertices.
-        for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
+        // Stage the current positions of the local vertices.
         const int nl = h0.y + h0.w;
         for (int i = threadIdx.x; i < nl; i += blockDim.x) {
             const int g = sidx[i];
@@ -238,8 +243,6 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             cp_async16(sd + i, S.pos + 2 * g + 1);
         }
         const bool active = lv < h0.y;
-        float4 tg = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (active) tg = S.tgt[h0.x + lv];
         if (threadIdx.x == 0) s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
         cp_async_wait_all();
         __syncthreads();
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             st_release_gpu(F.epoch + tile, epoch_base + k + 1);
         }
         task = s_next;
-        if (task < total) fetch_static(task, h0, h1, hv, roff);
+        if (task < total) fetch_static(task, h0, h1, hv, roff, tg);
     }
 }
 
