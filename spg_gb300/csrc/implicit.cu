@@ -230,9 +230,26 @@ __device__ __forceinline__ void block_reduce_add(double v, double *out)
     }
 }
 
+// Device-side control of one CG solve: the iteration loop runs as captured graphs of several
+// iterations with no host round trip per iteration; once done is set every later kernel of
+// the graph returns at once.
+struct CgControl {
+    int done;        // converged (|r|^2 < thr2) or out of iterations
+    int its;         // iterations taken
+    int max_its;
+    int pad;
+    double thr2;     // tol^2 |b|^2
+    double rr0;      // |b|^2
+    double rr;       // |r|^2 when done was set
+};
+
+__device__ __forceinline__ bool cg_done(const CgControl *c) { return c && *(volatile const int *)&c->done; }
+
 // Ap = A p (one thread per block row); with dots, dots[0] += p . Ap.
-__global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots)
+__global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots,
+                                     const CgControl *ctl = nullptr)
 {
+    if (cg_done(ctl)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double pap = 0.0;
     if (i < nv) {
@@ -271,10 +288,25 @@ __global__ void implicit_cg_init_kernel(const double *b, const double *dinv, dou
     block_reduce_add(rz, dots + 2);
 }
 
+// Eigen's start: nothing to do for b = 0; otherwise iterate while |r|^2 >= tol^2 |b|^2.
+__global__ void implicit_cg_control_kernel(CgControl *c, const double *dots, double tol, int max_its)
+{
+    const double rr0 = dots[1];
+    c->rr0 = rr0;
+    c->rr = rr0;
+    c->thr2 = fmax(tol * tol * rr0, 1e-300);
+    c->its = 0;
+    c->max_its = max_its;
+    c->done = (rr0 == 0.0 || rr0 < c->thr2 || max_its <= 0) ? 1 : 0;
+}
+
 // x += alpha p; r -= alpha Ap; z = D^-1 r; dots[1] += r.r, dots[2] += r.z (alpha = rz / pAp).
 __global__ void implicit_cg_update_kernel(double *x, double *r, double *z, const double *p, const double *Ap,
-                                         const double *dinv, int n, const double *prev, double *dots)
+                                         const double *dinv, int n, const double *prev, double *dots,
+                                         CgControl *ctl)
 {
+    if (cg_done(ctl)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ++ctl->its;  // read by the direction kernel
     const double alpha = prev[2] / prev[0];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0, rz = 0.0;
@@ -291,9 +323,22 @@ __global__ void implicit_cg_update_kernel(double *x, double *r, double *z, const
     block_reduce_add(rz, dots + 2);
 }
 
-// p = z + beta p, beta = rz_new / rz_old.
-__global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, const double *prev, const double *cur)
+// The iteration's stopping test (Eigen: |r|^2 < thr2 after the update, or the iteration
+// limit), then p = z + beta p with beta = rz_new / rz_old. Every block takes the same
+// decision: its inputs were written by earlier kernels.
+__global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, const double *prev, const double *cur,
+                                            CgControl *ctl)
 {
+    if (cg_done(ctl)) return;
+    const double rr = cur[1];
+    const bool stop = rr < ctl->thr2 || ctl->its >= ctl->max_its;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (stop) {
+            ctl->rr = rr;
+            ctl->done = 1;
+        }
+    }
+    if (stop) return;
     const double beta = cur[2] / prev[2];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -423,8 +468,9 @@ struct ImplicitSolver {
     cudaEvent_t ev0{nullptr}, ev1{nullptr};
     DevBuf d_idx, d_info, d_prm, d_eblk, d_row, d_col, d_val, d_diag, d_mass;
     DevBuf d_x, d_v, d_x0, d_v0, d_vi, d_xm1, d_vm1, d_f, d_b, d_u, d_w;
-    DevBuf d_dx, d_r, d_z, d_p, d_Ap, d_dinv, d_dots;
-    HostBuf h_dots;
+    DevBuf d_dx, d_r, d_z, d_p, d_Ap, d_dinv, d_dots, d_ctl;
+    HostBuf h_dots, h_ctl;
+    cudaGraphExec_t cg_graph{nullptr};
     ImplicitTables T{};
     int n_elem{0}, nnzb{0};
     // Step control of the robust methods (m_currentDt, m_consecutiveSuccessfulSteps) and the
@@ -435,6 +481,7 @@ struct ImplicitSolver {
 
     ~ImplicitSolver()
     {
+        if (cg_graph) cudaGraphExecDestroy(cg_graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) {
@@ -541,6 +588,8 @@ struct ImplicitSolver {
             SPGX_TRY_STATUS(b->alloc(vb));
         SPGX_TRY_STATUS(d_dots.alloc(size_t(8) * sizeof(double)));
         SPGX_TRY_STATUS(h_dots.alloc(size_t(8) * sizeof(double)));
+        SPGX_TRY_STATUS(d_ctl.alloc(sizeof(CgControl)));
+        SPGX_TRY_STATUS(h_ctl.alloc(sizeof(CgControl)));
         T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
                            d_col.as<int>(), d_val.as<double>(), d_diag.as<int>()};
         std::vector<double> x(3 * size_t(std::max(1, nv)), 0.0), v(x.size(), 0.0);
@@ -586,38 +635,69 @@ struct ImplicitSolver {
     // One CG solve of (alpha M + beta H) d_dx = d_b (ImplicitEulerBase::solveLinearSystem,
     // implicitEulerBase.cpp:227-239) with Eigen::ConjugateGradient's stopping rule
     // |r|^2 < tol^2 |b|^2. The BSR holds H on entry.
+    // The CG iterations as one graph of kCgChunk iterations (two parities of the dot-product
+    // slots per pair of iterations), replayed until the device-side control says done.
+    static constexpr int kCgChunk = 32;
+    spgx_status build_cg_graph()
+    {
+        const int nv = L.nv, n = n3();
+        double *A = d_dots.as<double>(), *B = A + 3;
+        CgControl *ctl = d_ctl.as<CgControl>();
+        cudaGraph_t g = nullptr;
+        SPGX_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < kCgChunk; ++it) {
+            double *prev = it % 2 == 0 ? A : B, *cur = it % 2 == 0 ? B : A;
+            cudaMemsetAsync(prev, 0, sizeof(double), stream);
+            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_p), vec(d_Ap), nv, prev, ctl);
+            cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream);
+            implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
+                                                                     vec(d_Ap), vec(d_dinv), n, prev, cur, ctl);
+            implicit_cg_direction_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_p), vec(d_z), n, prev, cur, ctl);
+        }
+        const cudaError_t ce = cudaStreamEndCapture(stream, &g);
+        if (ce != cudaSuccess) {
+            set_error(std::string("CG graph capture failed: ") + cudaGetErrorString(ce));
+            return SPGX_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&cg_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            set_error(std::string("CG graph instantiation failed: ") + cudaGetErrorString(ie));
+            return SPGX_ERR_CUDA;
+        }
+        return SPGX_OK;
+    }
+
+    // One CG solve of (alpha M + beta H) d_dx = d_b (ImplicitEulerBase::solveLinearSystem,
+    // implicitEulerBase.cpp:227-239) with Eigen::ConjugateGradient's stopping rule
+    // |r|^2 < tol^2 |b|^2. The BSR holds H on entry.
     spgx_status cg(double alpha, double beta, int &iterations, double &rel_residual)
     {
         const int nv = L.nv, n = n3();
         implicit_lhs_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_mass), nv, alpha, beta, vec(d_dinv));
-        double *dots = d_dots.as<double>();  // two sets of {pAp, rr, rz}: [0..2] previous, [3..5] current
-        double *hd = h_dots.as<double>();
+        double *dots = d_dots.as<double>();  // two sets of {pAp, rr, rz}: [0..2] and [3..5]
         SPGX_CUDA(cudaMemsetAsync(dots, 0, 6 * sizeof(double), stream));
         implicit_cg_init_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_b), vec(d_dinv), vec(d_dx), vec(d_r), vec(d_z),
                                                                 vec(d_p), n, dots);
-        SPGX_CUDA(cudaMemcpyAsync(hd, dots, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
-        SPGX_CUDA(cudaStreamSynchronize(stream));
-        const double rhs2 = hd[1];
-        iterations = 0;
-        rel_residual = 0.0;
-        if (rhs2 == 0.0) return SPGX_OK;  // x = 0
-        const double thr2 = std::max(P.cg_threshold * P.cg_threshold * rhs2, 1e-300);
-        double rr = rhs2;
-        double *prev = dots, *cur = dots + 3;
-        while (rr >= thr2 && iterations < P.cg_max_iterations) {
-            SPGX_CUDA(cudaMemsetAsync(prev, 0, sizeof(double), stream));
-            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_p), vec(d_Ap), nv, prev);
-            SPGX_CUDA(cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream));
-            implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
-                                                                     vec(d_Ap), vec(d_dinv), n, prev, cur);
-            implicit_cg_direction_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_p), vec(d_z), n, prev, cur);
-            SPGX_CUDA(cudaMemcpyAsync(hd, cur, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        implicit_cg_control_kernel<<<1, 1, 0, stream>>>(d_ctl.as<CgControl>(), dots, P.cg_threshold,
+                                                        P.cg_max_iterations);
+        SPGX_CUDA(cudaGetLastError());
+        if (!cg_graph) SPGX_TRY_STATUS(build_cg_graph());
+        const CgControl *hc = h_ctl.as<CgControl>();
+        const int max_launches = P.cg_max_iterations / kCgChunk + 2;
+        for (int k = 0; k < max_launches; ++k) {
+            SPGX_CUDA(cudaGraphLaunch(cg_graph, stream));
+            SPGX_CUDA(cudaMemcpyAsync(h_ctl.as<void>(), d_ctl.as<void>(), sizeof(CgControl), cudaMemcpyDeviceToHost,
+                                      stream));
             SPGX_CUDA(cudaStreamSynchronize(stream));
-            rr = hd[1];
-            ++iterations;
-            std::swap(prev, cur);
+            if (hc->done) break;
         }
-        rel_residual = std::sqrt(rr / rhs2);
+        if (!hc->done) {
+            set_error("internal: the CG control did not finish");
+            return SPGX_ERR_CUDA;
+        }
+        iterations = hc->its;
+        rel_residual = hc->rr0 > 0.0 ? std::sqrt(hc->rr / hc->rr0) : 0.0;
         return SPGX_OK;
     }
 
