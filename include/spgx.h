@@ -259,6 +259,11 @@ spgx_status spgx_vbd_get_launch(spgx_vbd *h, int32_t *kernel, int32_t *lanes_per
  * one-stencil SpringAnchorEnergy appended after the object's energies would. Takes effect at
  * the next step, with no rebuild of colours, incidences or tiles (an anchor adds no graph
  * edge, so the reference's recolouring gives the same colours). n = 0 removes every pick. */
+/* Failure-detection test hook (dataflow kernel only): marks one tile's sweep counter as never
+ * reached, so that the next step's waits on that tile run out their bounded polls (about a
+ * second). Every CTA then leaves the kernel, the step returns SPGX_ERR_TIMEOUT, the
+ * counters are reset, and the handle keeps working; nothing faults or hangs. */
+spgx_status spgx_vbd_test_stall_tile(spgx_vbd *h, int32_t tile);
 #define SPGX_MAX_PICKS 16
 spgx_status spgx_vbd_set_picks(spgx_vbd *h, int32_t n, const int32_t *object, const int32_t *vertex,
                                const double *target, const double *stiffness);

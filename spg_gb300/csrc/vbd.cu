@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
 // they in turn wait for T. Each task waits only on tasks with smaller tickets, all held by
 // co-resident CTAs (cooperative launch), so the waits always end; each is still bounded, and
 // a wait that gives up sets the abort flag and status bit 1 so that every CTA leaves.
-constexpr int kFlowMaxPolls = 1 << 22;  // with 128 ns sleeps: about a second per wait
+constexpr int kFlowMaxPolls = 1 << 21;  // with 128 ns sleeps and an L2 round trip: about a second per wait
 
 template <int G>
 __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V, const DevState S,
@@ -1418,6 +1418,29 @@ spgx_status spgx_vbd_set_picks(spgx_vbd *h, int32_t n, const int32_t *object, co
     }
     SPGX_CUDA(cudaSetDevice(h->s->device));
     return h->s->set_picks(n, object, vertex, target, stiffness);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_test_stall_tile(spgx_vbd *h, int32_t tile)
+{
+    SPGX_GUARD_BEGIN
+    if (!h) {
+        spgx::set_error("NULL solver handle");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    auto &s = *h->s;
+    const int n_tiles = s.TL.color_tiles.empty() ? 0 : s.TL.color_tiles.back();
+    if (s.kernel != 3 || tile < 0 || tile >= n_tiles) {
+        spgx::set_error("the handle does not run the dataflow kernel, or no such tile");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    SPGX_CUDA(cudaSetDevice(s.device));
+    // A sweep counter no sweep ever reaches: every task that reads this tile waits until its
+    // bounded poll gives up.
+    const int never = -(1 << 30);
+    SPGX_CUDA(cudaMemcpyAsync(s.fl_epoch.as<int>() + tile, &never, sizeof(int), cudaMemcpyHostToDevice, s.stream));
+    SPGX_CUDA(cudaStreamSynchronize(s.stream));
+    return SPGX_OK;
     SPGX_GUARD_END
 }
 

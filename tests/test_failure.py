@@ -1,0 +1,50 @@
+"""Failure detection without a GPU fault: a bounded device-side wait that runs out is
+reported as a status, and the solver keeps working (the dataflow kernel's tile waits)."""
+import time
+
+import numpy as np
+import pytest
+
+from tests import scenes
+
+pytestmark = pytest.mark.gpu
+
+N = pytest.importorskip("spg_gb300.native")
+SPGX_ERR_TIMEOUT = 5
+
+
+def test_dataflow_wait_runs_out_and_the_solver_recovers():
+    obj = scenes.spring_cloth_cfg3(65)
+    kw = dict(dt=1 / 120, iterations=20, gravity=scenes.GRAVITY, kernel=3)
+    s = N.VbdSolver([obj], **kw)
+    k, g, b = s.launch()
+    assert k == 3
+    twin = N.VbdSolver([obj], lanes_per_vertex=g, tile_vertices=b // g, **kw)
+    assert twin.launch() == (k, g, b)
+    s.step()
+    twin.step()
+    x0, v0 = s.state(0)
+    # Both take the state through the FP64 host arrays (which drops delta bits below 2^-53 of
+    # the position), so that their device representations match from here on.
+    twin.set_state(0, *twin.state(0))
+    s.test_stall_tile(3)   # a sweep counter nothing will ever reach
+    t0 = time.time()
+    with pytest.raises(N.SpgxError) as err:
+        s.step()
+    elapsed = time.time() - t0
+    assert err.value.status == SPGX_ERR_TIMEOUT, err.value
+    assert elapsed < 30, elapsed
+    # The handle still works: from the state before the failed step it steps exactly like a
+    # twin solver that never stalled.
+    s.set_state(0, x0, v0)
+    s.step()
+    twin.step()
+    assert np.array_equal(s.state(0)[0], twin.state(0)[0])
+    print(f"stalled step returned after {elapsed:.2f} s")
+
+
+def test_stall_hook_needs_the_dataflow_kernel():
+    obj = scenes.spring_cloth_cfg3(9)
+    s = N.VbdSolver([obj], dt=1 / 120, iterations=1, gravity=scenes.GRAVITY, kernel=1)
+    with pytest.raises(N.SpgxError):
+        s.test_stall_tile(0)
