@@ -161,18 +161,24 @@ __device__ __noinline__ void xpbd_generic(const DevTables &T, float4 *pos, const
     }
 }
 
-__global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, float4 *pos, const float *__restrict__ invm,
-                                                         const int *__restrict__ items, int n, float invh2)
+// Projects the constraints of one work item (one stencil).
+// Type paths a kernel instance carries, beyond springs, bending and anchors: the register
+// budget of a kernel is that of its heaviest path, so scenes without the heavy types run a
+// lighter instance.
+constexpr int kPathGeneric = 1, kPathStvk = 2, kPathSnh = 4;
+
+template <int kPaths>
+__device__ __forceinline__ void project_item(const DevTables &T, float4 *pos, const float *__restrict__ invm, int item,
+                                             float invh2)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int item = __ldg(items + t);
     const int type = (item >> kItemShift) & 7;
     const int e = item & kItemMask;
-    if (type == kItemGeneric) {
+    if ((kPaths & kPathGeneric) && type == kItemGeneric) {
         xpbd_generic(T, pos, invm, e, invh2);
         return;
     }
+    if (!(kPaths & kPathStvk) && type == SPGX_ENERGY_MEMBRANE_STVK) return;
+    if (!(kPaths & kPathSnh) && type == SPGX_ENERGY_STABLE_NEO_HOOKEAN) return;
     switch (type) {
     case SPGX_ENERGY_SPRING: {
         // SpringEnergy::projectPosition, springEnergy.cpp:48-68
@@ -212,6 +218,7 @@ __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, floa
         break;
     }
     case SPGX_ENERGY_MEMBRANE_STVK: {
+        if (!(kPaths & kPathStvk)) break;
         const int4 st = __ldg(T.stvk_idx + e);
         const float4 D4 = __ldg(T.stvk_D + e);
         const float4 Ca = __ldg(T.stvk_Ca + e), Cb = __ldg(T.stvk_Cb + e);
@@ -234,6 +241,7 @@ __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, floa
         break;
     }
     default: {
+        if (!(kPaths & kPathSnh)) break;
         const int4 st = __ldg(T.snh_idx + e);
         const float4 a = __ldg(T.snh_p0 + e), b = __ldg(T.snh_p1 + e), c = __ldg(T.snh_p2 + e);
         const float2 cm = __ldg(T.snh_cmp + e);
@@ -260,12 +268,10 @@ __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, floa
 // Anchors are projected by their own kernel because their stencil is a single vertex that is
 // not part of the element record (StencilBlockEnergy::projectPosition with the anchor
 // constraint, springAnchorEnergy.cpp:8-19).
-__global__ void xpbd_anchor_kernel(const DevTables T, const int *__restrict__ anchor_v, float4 *pos,
-                                   const float *__restrict__ invm, const int *__restrict__ items, int n, float invh2)
+__device__ __forceinline__ void project_anchor(const DevTables &T, const int *__restrict__ anchor_v, float4 *pos,
+                                               const float *__restrict__ invm, int item, float invh2)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const int e = __ldg(items + t) & kItemMask;
+    const int e = item & kItemMask;
     const float4 a = __ldg(T.anchors + e);
     const int v = __ldg(anchor_v + e);
     const V3f xa = (v3(pos[2 * v]) - mk(a.x, a.y, a.z)) + v3(pos[2 * v + 1]);
@@ -276,6 +282,21 @@ __global__ void xpbd_anchor_kernel(const DevTables T, const int *__restrict__ an
     const int idx[1] = {v};
     const float cmp[1] = {__ldg(T.anchor_cmp + e).x};
     project_block<1, 1>(pos, idx, w, C, g, cmp, invh2);
+}
+
+template <int kPaths>
+__global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, float4 *pos, const float *__restrict__ invm,
+                                                         const int *__restrict__ items, int n, float invh2)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) project_item<kPaths>(T, pos, invm, __ldg(items + t), invh2);
+}
+
+__global__ void xpbd_anchor_kernel(const DevTables T, const int *__restrict__ anchor_v, float4 *pos,
+                                   const float *__restrict__ invm, const int *__restrict__ items, int n, float invh2)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) project_anchor(T, anchor_v, pos, invm, __ldg(items + t), invh2);
 }
 
 struct XpbdPhase {
@@ -299,6 +320,7 @@ struct XpbdSolver {
     DevBuf d_items, d_anchor_v;
     DevTables T{};
     std::vector<XpbdPhase> phases;
+    int paths{0};  // kPath* bits of the scene's energy types
 
     ~XpbdSolver()
     {
@@ -384,7 +406,29 @@ struct XpbdSolver {
             }
         }
         SPGX_TRY_STATUS(d_items.upload(items));
+        return setup_paths();
+    }
+
+    // The kernel instance carries only the type paths the scene needs.
+    spgx_status setup_paths()
+    {
+        paths = (L.el.gen_idx.empty() ? 0 : kPathGeneric) | (L.el.stvk_idx.empty() ? 0 : kPathStvk) |
+                (L.el.snh_idx.empty() ? 0 : kPathSnh);
         return SPGX_OK;
+    }
+
+    void launch_phase(int grid, cudaStream_t st, const int *items, int n, float invh2)
+    {
+        switch (paths) {
+        case 0: xpbd_phase_kernel<0><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 1: xpbd_phase_kernel<1><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 2: xpbd_phase_kernel<2><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 3: xpbd_phase_kernel<3><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 4: xpbd_phase_kernel<4><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 5: xpbd_phase_kernel<5><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 6: xpbd_phase_kernel<6><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        default: xpbd_phase_kernel<7><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        }
     }
 
     void launch_phases(cudaStream_t st)
@@ -396,8 +440,7 @@ struct XpbdSolver {
                 xpbd_anchor_kernel<<<grid, block, 0, st>>>(T, d_anchor_v.as<int>(), X.pos(), X.invm(),
                                                            d_items.as<int>() + ph.offset, ph.count, invh2);
             else
-                xpbd_phase_kernel<<<grid, block, 0, st>>>(T, X.pos(), X.invm(), d_items.as<int>() + ph.offset,
-                                                          ph.count, invh2);
+                launch_phase(grid, st, d_items.as<int>() + ph.offset, ph.count, invh2);
         }
     }
 
@@ -448,6 +491,7 @@ struct XpbdSolver {
         SPGX_CUDA(cudaEventRecord(ev1, stream));
         SPGX_CUDA(cudaGetLastError());
         SPGX_CUDA(cudaStreamSynchronize(stream));
+
         float ms = 0.f;
         SPGX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         if (stats) {
