@@ -320,13 +320,22 @@ spgx_status spgx_mlp_train(spgx_mlp *h, int32_t n, const float *x, const float *
 
 /* Chooses the initial guess of every substep: mode 0 the inertial guess y (the reference's);
  * mode 1 the learned guess (mlp required); mode 2 the previous step's acceleration carried
- * over, x_w = x_n + 2 (x_n - x_{n-1}) - (x_{n-1} - x_{n-2}) (no network; a baseline for
- * the learned guess). Modes 1 and 2 keep their candidate only when it lowers the residual.
+ * over, x_e = x_n + 2 (x_n - x_{n-1}) - (x_{n-1} - x_{n-2}) (no network; a baseline for
+ * the learned guess). Mode 2 keeps x_e only when its residual is below y's. Mode 1 forms
+ * x_w = x_e + l * smoothed network correction, runs 20 sweeps from each of x_w and x_e, and
+ * continues from the one with the lower residual (the sweeps of the other one are spent and
+ * counted in spgx_step_stats.iterations; residual_warm / residual_extrapolated are the
+ * residuals after those sweeps).
  * The first call also starts keeping the displacement history (from then on, and after
  * every set_state/reset, seeded with a constant-velocity past). The network must outlive
  * its use by the solver and live on the solver's device; do not train it while the solver
  * steps. */
 spgx_status spgx_vbd_set_warm_start(spgx_vbd *h, const spgx_mlp *mlp, int32_t mode);
+/* Smoothing passes applied to the network's correction field before the learned guess is
+ * formed: each pass replaces a vertex's correction by the mean of itself and its one-ring
+ * mean. 0 to 64; the default is 20. The network's error is mostly per-vertex noise, which the
+ * stiff springs turn into large forces; the smoothed field keeps its smooth, accurate part. */
+spgx_status spgx_vbd_set_warm_start_smoothing(spgx_vbd *h, int32_t passes);
 /* One step (one substep only; history started by spgx_vbd_set_warm_start) that also returns,
  * for every vertex of the scene in the solver's internal order, the features at the start of
  * the step (features[n_vertices][24]) and (x - y) / l at its end (targets[n_vertices][3]);

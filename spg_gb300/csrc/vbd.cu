@@ -480,6 +480,7 @@ static void launch_flow(const VbdSolver &s, int n, cudaStream_t st)
 
 static void launch_iterations(const VbdSolver &s, int n, cudaStream_t st)
 {
+    if (n <= 0) return;
     if (s.kernel == 3) {
         launch_flow(s, n, st);
         return;
@@ -966,7 +967,7 @@ spgx_status VbdSolver::build_graph()
     for (int s = 0; s < P.substeps; ++s) {
         launch_begin(*this, stream);
         if (W.mode != kWarmInertial) launch_warm(stream);
-        launch_iterations(*this, P.iterations, stream);
+        launch_iterations(*this, P.iterations - warm_probe_sweeps(), stream);
         launch_end(*this, stream);
     }
     const cudaError_t ce = cudaStreamEndCapture(stream, &g);
@@ -1037,24 +1038,38 @@ spgx_status VbdSolver::residual_norm(double *out)
 }
 
 // Initial guess of one substep, after the inertial predict, all on the stream with no host
-// round trip. wres[0] = ||r(y)||^2. Extrapolated mode: wres[1] = ||r(x_e)||^2. Learned mode:
-// wres[2] = ||r(x_e)||^2 and wres[1] = ||r(x_e + l MLP)||^2. The substep then starts from the
-// guess with the lowest residual, so the network can only help.
-void VbdSolver::launch_warm(cudaStream_t st)
+// round trip. wres[0] = ||r(y)||^2.
+// Extrapolated mode: wres[1] = ||r(x_e)||^2, and the substep starts from the better of y and x_e.
+// Learned mode: the residual of a guess right after the jump weighs its high-frequency error
+// (per-vertex noise stretches the stiff springs) far above its smooth error, which the sweeps
+// remove first; the learned guess x_e + l MLP has much lower error overall but a higher
+// initial residual. So each of x_w and x_e first runs kWarmProbeSweeps sweeps: wres[1] and
+// wres[2] are the residuals after them, and the substep continues from the better state (the
+// other probe's sweeps are spent). Returns the sweeps the probes ran.
+int VbdSolver::launch_warm(cudaStream_t st)
 {
     double *wres = W.wres.as<double>();
     cudaMemsetAsync(wres, 0, 3 * sizeof(double), st);
     launch_residual(*this, st, wres);
-    const bool learned = W.mode == kWarmLearned;
     launch_warm_extrapolate(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, st);
-    launch_residual(*this, st, wres + (learned ? 2 : 1));
-    if (learned) {
-        launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, st);
-        W.mlp->infer(W.feats.as<float>(), L.nv, W.out.as<float>(), st);
-        launch_warm_apply(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, st);
+    if (W.mode != kWarmLearned) {
         launch_residual(*this, st, wres + 1);
+        launch_warm_select(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, false, d_counters.as<int>(), st);
+        return 0;
     }
-    launch_warm_select(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, learned, d_counters.as<int>(), st);
+    const int probe = warm_probe_sweeps();
+    launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, st);
+    W.mlp->infer(W.feats.as<float>(), L.nv, W.out.as<float>(), st);
+    launch_warm_smooth(W, L.nv, st);
+    launch_warm_apply(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, st);
+    launch_iterations(*this, probe, st);
+    launch_residual(*this, st, wres + 1);
+    cudaMemcpyAsync(d_backup.as<void>(), X.pos(), size_t(L.nv) * 2 * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+    launch_warm_extrapolate(W, X.pos(), X.tgt(), X.vel(), L.nv, h_sub, P.gravity, st);
+    launch_iterations(*this, probe, st);
+    launch_residual(*this, st, wres + 2);
+    launch_warm_probe_select(W, X.pos(), d_backup.as<float4>(), L.nv, d_counters.as<int>(), st);
+    return 2 * probe;
 }
 
 // Uploads positions/velocities set from the host; a replaced state restarts the displacement
@@ -1082,6 +1097,7 @@ spgx_status VbdSolver::enable_history()
     SPGX_TRY_STATUS(W.vhist.alloc(n * sizeof(float4)));
     SPGX_TRY_STATUS(W.feats.alloc(n * kWarmFeatures * sizeof(float)));
     SPGX_TRY_STATUS(W.out.alloc(n * 3 * sizeof(float)));
+    SPGX_TRY_STATUS(W.out2.alloc(n * 3 * sizeof(float)));
     SPGX_TRY_STATUS(W.wres.alloc(3 * sizeof(double)));
     // No earlier motion is known: take the previous step's displacement equal to the current
     // velocity's (constant-velocity history).
@@ -1137,17 +1153,19 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
             for (int s = 0; s < P.substeps; ++s) {
                 launch_begin(*this, stream);
                 if (W.mode != kWarmInertial) launch_warm(stream);
-                launch_iterations(*this, P.iterations, stream);
+                launch_iterations(*this, P.iterations - warm_probe_sweeps(), stream);
                 launch_end(*this, stream);
             }
         }
-        st.iterations = P.iterations * P.substeps;
+        // The probe of the guess that was not kept adds its sweeps.
+        st.iterations = (P.iterations + warm_probe_sweeps()) * P.substeps;
         st.converged = 1;
     } else {
         st.converged = 1;
         for (int s = 0; s < P.substeps; ++s) {
             launch_begin(*this, stream);
             double r0 = 0, r = 0;
+            int probe = 0;  // sweeps already applied to the state the substep continues from
             if (W.mode != kWarmInertial) {
                 launch_warm(stream);
                 SPGX_CUDA(cudaMemcpyAsync(hw, W.wres.as<double>(), 3 * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1157,7 +1175,9 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
                 r0 = std::sqrt(hw[0]);
                 st.residual_warm = std::sqrt(hw[1]);
                 st.residual_extrapolated = std::sqrt(learned ? hw[2] : hw[1]);
-                r = std::sqrt(std::min(hw[0], std::min(hw[1], learned ? hw[2] : hw[1])));
+                r = std::sqrt(learned ? std::min(hw[1], hw[2]) : std::min(hw[0], hw[1]));
+                probe = warm_probe_sweeps();
+                st.iterations += probe;  // the probe that was not kept
             } else {
                 if (P.tolerance > 0) SPGX_TRY_STATUS(residual_norm(&r0));
                 r = r0;
@@ -1166,7 +1186,7 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
             // computed them already.
             if (record && W.mode != kWarmLearned) launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, stream);
             if (P.tolerance > 0) {
-                int it = 0;
+                int it = probe;
                 while (it < P.max_iterations && r > P.tolerance * r0) {
                     const int chunk = std::min(P.check_interval, P.max_iterations - it);
                     launch_iterations(*this, chunk, stream);
@@ -1178,7 +1198,7 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
                 st.residual_initial = r0;
                 st.residual_final = r;
             } else {
-                launch_iterations(*this, P.iterations, stream);
+                launch_iterations(*this, P.iterations - probe, stream);
                 st.iterations += P.iterations;
             }
             if (record) launch_warm_targets(X.pos(), X.tgt(), L.nv, h_sub, W.out.as<float>(), stream);
@@ -1418,6 +1438,19 @@ spgx_status spgx_vbd_set_picks(spgx_vbd *h, int32_t n, const int32_t *object, co
     }
     SPGX_CUDA(cudaSetDevice(h->s->device));
     return h->s->set_picks(n, object, vertex, target, stiffness);
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_vbd_set_warm_start_smoothing(spgx_vbd *h, int32_t passes)
+{
+    SPGX_GUARD_BEGIN
+    if (!h || passes < 0 || passes > 64) {
+        spgx::set_error("smoothing passes must be in [0, 64]");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    h->s->W.smooth = passes;
+    h->s->graph_valid = false;
+    return SPGX_OK;
     SPGX_GUARD_END
 }
 

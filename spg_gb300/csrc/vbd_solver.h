@@ -76,7 +76,13 @@ struct VbdSolver {
     spgx_status enable_history();
     spgx_status upload_state();
     spgx_status set_warm_start(const Mlp *mlp, int mode);
-    void launch_warm(cudaStream_t st);
+    int launch_warm(cudaStream_t st);
+    // Sweeps each probe of the learned guess runs (0 in the other modes).
+    int warm_probe_sweeps() const
+    {
+        if (W.mode != kWarmLearned) return 0;
+        return std::min(kWarmProbeSweeps, P.tolerance > 0 ? P.max_iterations : P.iterations);
+    }
     // Replaces the dynamic anchors (picking) between steps.
     spgx_status set_picks(int n, const int32_t *object, const int32_t *vertex, const double *target, const double *k);
 };

@@ -175,6 +175,17 @@ __global__ void warm_select_kernel(float4 *__restrict__ pos, const float4 *__res
     }
 }
 
+__global__ void warm_probe_select_kernel(float4 *__restrict__ pos, const float4 *__restrict__ saved,
+                                         const double *__restrict__ wres, int nv, int *counters)
+{
+    const bool learned = wres[1] < wres[2];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) atomicAdd(counters + (learned ? 3 : 4), 1);
+    if (!learned || i >= nv) return;
+    pos[2 * i] = saved[2 * i];
+    pos[2 * i + 1] = saved[2 * i + 1];
+}
+
 __global__ void warm_targets_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ tgt, int nv,
                                     float inv_ell, float *__restrict__ T)
 {
@@ -196,6 +207,39 @@ void launch_warm_features(const WarmStart &W, const float4 *vel, int nv, double 
         vel, W.vhist.as<float4>(), W.nbr_off.as<int>(), W.nbr.as<int>(), W.stat.as<float4>(), nv, a,
         float(h * g[0]), float(h * g[1]), float(h * g[2]), float(g[0] / kWarmG0), float(g[1] / kWarmG0),
         float(g[2] / kWarmG0), W.feats.as<float>());
+}
+
+__global__ void warm_smooth_kernel(const float *__restrict__ in, float *__restrict__ out, const int *__restrict__ off,
+                                   const int *__restrict__ nbr, int nv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int b = off[i], e = off[i + 1];
+    float m[3] = {0.f, 0.f, 0.f};
+    for (int k = b; k < e; ++k) {
+        const float *o = in + 3 * size_t(nbr[k]);
+        m[0] += o[0];
+        m[1] += o[1];
+        m[2] += o[2];
+    }
+    const float inv = e > b ? 1.f / float(e - b) : 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float s = in[3 * size_t(i) + c];
+        out[3 * size_t(i) + c] = e > b ? 0.5f * (s + m[c] * inv) : s;
+    }
+}
+
+void launch_warm_smooth(const WarmStart &W, int nv, cudaStream_t st)
+{
+    if (nv == 0 || W.smooth <= 0) return;
+    float *a = W.out.as<float>(), *b = W.out2.as<float>();
+    for (int p = 0; p < W.smooth; ++p) {
+        warm_smooth_kernel<<<grid_for(nv), 256, 0, st>>>(a, b, W.nbr_off.as<int>(), W.nbr.as<int>(), nv);
+        std::swap(a, b);
+    }
+    if (a != W.out.as<float>())
+        cudaMemcpyAsync(W.out.as<float>(), a, size_t(nv) * 3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
 }
 
 void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
@@ -222,6 +266,13 @@ void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, cons
     warm_select_kernel<<<grid_for(nv), 256, 0, st>>>(pos, tgt, vel, W.vhist.as<float4>(), W.wres.as<double>(), nv,
                                                      three_way, float(h), float(h * g[0]), float(h * g[1]),
                                                      float(h * g[2]), counters);
+}
+
+void launch_warm_probe_select(const WarmStart &W, float4 *pos, const float4 *saved, int nv, int *counters,
+                              cudaStream_t st)
+{
+    warm_probe_select_kernel<<<grid_for(std::max(1, nv)), 256, 0, st>>>(pos, saved, W.wres.as<double>(), nv,
+                                                                       counters);
 }
 
 void launch_warm_targets(const float4 *pos, const float4 *tgt, int nv, double h, float *targets, cudaStream_t st)

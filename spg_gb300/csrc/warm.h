@@ -29,6 +29,10 @@ namespace spgx {
 
 constexpr int kWarmFeatures = 24;
 constexpr double kWarmG0 = 9.81;
+// Sweeps run from each of the learned and the extrapolated guess before they are compared.
+constexpr int kWarmProbeSweeps = 20;
+// Default one-ring smoothing passes over the network's correction field.
+constexpr int kWarmSmoothPasses = 20;
 
 struct Mlp;
 
@@ -44,11 +48,15 @@ struct WarmStart {
     bool history{false};  // history buffers exist and are maintained every substep
     int mode{kWarmInertial};
     const Mlp *mlp{nullptr};
-    DevBuf nbr_off, nbr, stat, vhist, feats, out, wres;
+    int smooth{kWarmSmoothPasses};  // one-ring smoothing passes over the network's correction field
+    DevBuf nbr_off, nbr, stat, vhist, feats, out, out2, wres;
 };
 
 // feats = features of every vertex at the start of the substep (after the inertial predict).
 void launch_warm_features(const WarmStart &W, const float4 *vel, int nv, double h, const double *g, cudaStream_t st);
+// W.smooth passes of out <- (out + one-ring mean of out) / 2 (the network's correction field
+// keeps its smooth part and loses per-vertex noise, which the stiff springs amplify).
+void launch_warm_smooth(const WarmStart &W, int nv, cudaStream_t st);
 // delta = tgt + h (v_n - v_{n-1}) - h^2 g + l * out for every vertex (the learned guess).
 void launch_warm_apply(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
                        const double *g, cudaStream_t st);
@@ -60,6 +68,11 @@ void launch_warm_extrapolate(const WarmStart &W, float4 *pos, const float4 *tgt,
 // (wres[2]). Counts the pick in counters[3] (learned) or counters[4] (extrapolated).
 void launch_warm_select(const WarmStart &W, float4 *pos, const float4 *tgt, const float4 *vel, int nv, double h,
                         const double *g, bool three_way, int *counters, cudaStream_t st);
+// The learned guess's probe: when wres[1] (its residual after the probe sweeps) is below
+// wres[2] (the extrapolated guess's), the positions go back to the learned probe's state
+// saved in `saved` (base and delta per vertex); counts the pick in counters[3] or [4].
+void launch_warm_probe_select(const WarmStart &W, float4 *pos, const float4 *saved, int nv, int *counters,
+                              cudaStream_t st);
 // targets = (x - y) / l for every vertex (training data of the converged step).
 void launch_warm_targets(const float4 *pos, const float4 *tgt, int nv, double h, float *targets, cudaStream_t st);
 

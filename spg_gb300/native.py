@@ -107,6 +107,7 @@ def lib():
         L.spgx_vbd_get_launch.argtypes = [vp, ip, ip, ip]
         L.spgx_vbd_set_picks.argtypes = [vp, i32, ip, ip, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.spgx_vbd_test_stall_tile.argtypes = [vp, i32]
+        L.spgx_vbd_set_warm_start_smoothing.argtypes = [vp, i32]
         L.spgx_vbd_profile_sweeps.argtypes = [vp, i32, dp]
         L.spgx_eval_vertex_blocks.argtypes = [i32, i32, dp, dp, ip, dp, dp]
         L.spgx_eval_constraints.argtypes = [i32, i32, dp, dp, dp, dp]
@@ -316,6 +317,10 @@ class VbdSolver:
         o, v, t, k = (np.ascontiguousarray(a) for a in (o, v, t, k))
         check(lib().spgx_vbd_set_picks(self.h, n, _p(o, C.c_int32), _p(v, C.c_int32), _p(t, C.c_double),
                                        _p(k, C.c_double)))
+
+    def set_warm_start_smoothing(self, passes):
+        """One-ring smoothing passes over the network's correction before the learned guess."""
+        check(lib().spgx_vbd_set_warm_start_smoothing(self.h, passes))
 
     def test_stall_tile(self, tile):
         """Failure-detection test hook: the next dataflow step's waits on `tile` run out."""

@@ -78,10 +78,10 @@ def test_extrapolated_guess_cuts_iterations_to_tolerance():
 
 @pytest.mark.gpu
 def test_learned_guess_with_the_shipped_network():
-    """The learned mode (extrapolation plus the shipped network's correction, started from
-    the lowest-residual guess) reaches the tolerance in at most 2/3 of the inertial guess's
-    iterations, and never needs more than the extrapolated guess alone by more than the
-    check granularity."""
+    """The learned mode (extrapolation plus the shipped network's correction; 20 sweeps from
+    each of the two guesses, then the lower residual continues) reaches the tolerance in at
+    most 2/3 of the inertial guess's iterations, and never needs more than the extrapolated
+    guess alone by more than the check granularity (the counts include both probes)."""
     mlp = W.load_mlp()
     plain, _ = _iterations(0)
     learned, picks = _iterations(1, mlp)
