@@ -249,65 +249,79 @@ def _timed_steps(solver, steps):
     return [solver.step().device_ms for _ in range(steps)]
 
 
-def other_configs(local) -> dict:
+def other_configs(local, only=None) -> dict:
     """The other benchmark configurations, each timed with CUDA events on its solver's stream
-    (vertex-solves/s = vertices x iterations / device time; XPBD in steps/s)."""
+    (vertex-solves/s = vertices x iterations / device time; XPBD in steps/s). With `only`,
+    just the configuration of that name (a single case for profiling)."""
     from spg_gb300 import native as N
     from spg_gb300 import scenes as S
+
+    def want(name):
+        return only is None or only == name
+
     out = {}
     cloth = S.cloth(33).objects[0]
-    s = N.VbdSolver([cloth], dt=1 / 60, iterations=100, gravity=GRAVITY, device=local)
-    ms = statistics.mean(_timed_steps(s, 10))
-    out["cloth_33x33_stvk_100it"] = {"vertex_solves_per_s": cloth.nv * 100 / (ms * 1e-3), "ms_per_step": ms,
-                                     "launch": list(s.launch())}
-    s.close()
     beam = S.tet_beam().objects[0]
-    s = N.VbdSolver([beam], dt=1 / 60, iterations=50, gravity=GRAVITY, device=local)
-    ms = statistics.mean(_timed_steps(s, 10))
-    out["snh_beam_41x11x11_50it"] = {"vertex_solves_per_s": beam.nv * 50 / (ms * 1e-3), "ms_per_step": ms,
-                                     "launch": list(s.launch())}
-    s.close()
-    batch = S.patch_batch(512, 16, 128, seed=2024).objects
-    nv = sum(o.nv for o in batch)
-    s = N.VbdSolver(batch, dt=1 / 60, iterations=30, gravity=GRAVITY, device=local)
-    ms = statistics.mean(_timed_steps(s, 5))
-    out["batch_512_patches_30it"] = {"vertex_solves_per_s": nv * 30 / (ms * 1e-3), "ms_per_step": ms,
-                                     "vertices": nv, "colors": int(s.n_colors(-1)), "launch": list(s.launch()),
-                                     "graph": True}
-    s.close()
-    imp = N.ImplicitSolver([cloth], dt=1 / 60, substeps=1, gravity=GRAVITY, device=local)
-    stats = [imp.step() for _ in range(8)][3:]
-    out["implicit_euler_cloth_33x33"] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
-                                         "cg_iterations": [int(st.iterations) for st in stats],
-                                         "precision": "FP64 assembly and CG"}
-    imp.close()
-    big = S.spring_cloth(ROWS).objects[0]
-    imp = N.ImplicitSolver([big], dt=DT, substeps=1, gravity=GRAVITY, device=local)
-    stats = [imp.step() for _ in range(4)][1:]
-    out["implicit_euler_spring_cloth_513"] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
-                                              "cg_iterations": [int(st.iterations) for st in stats],
-                                              "converged": [bool(st.converged) for st in stats],
-                                              "precision": "FP64 assembly and CG"}
-    imp.close()
-    names = ["newton_dx", "newton_dv", "newton_robust", "baraff_witkin", "bdf2", "static_newton",
-             "quasi_static_newton", "quasi_static_newton_robust", "symplectic_euler"]
-    solvers = {}
-    for method, name in enumerate(names):
-        dt = 1e-4 if name == "symplectic_euler" else 1 / 60
-        imp = N.ImplicitSolver([beam], dt=dt, substeps=1, gravity=GRAVITY, device=local, method=method)
-        stats = [imp.step() for _ in range(5)][2:]
-        solvers[name] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
-                         "cg_iterations": [int(st.iterations) for st in stats]}
+    big = S.spring_cloth(ROWS).objects[0] if (only is None or "513" in only) else None
+    if want("cloth_33x33_stvk_100it"):
+        s = N.VbdSolver([cloth], dt=1 / 60, iterations=100, gravity=GRAVITY, device=local)
+        ms = statistics.mean(_timed_steps(s, 10))
+        out["cloth_33x33_stvk_100it"] = {"vertex_solves_per_s": cloth.nv * 100 / (ms * 1e-3), "ms_per_step": ms,
+                                         "launch": list(s.launch())}
+        s.close()
+    if want("snh_beam_41x11x11_50it"):
+        s = N.VbdSolver([beam], dt=1 / 60, iterations=50, gravity=GRAVITY, device=local)
+        ms = statistics.mean(_timed_steps(s, 10))
+        out["snh_beam_41x11x11_50it"] = {"vertex_solves_per_s": beam.nv * 50 / (ms * 1e-3), "ms_per_step": ms,
+                                         "launch": list(s.launch())}
+        s.close()
+    if want("batch_512_patches_30it"):
+        batch = S.patch_batch(512, 16, 128, seed=2024).objects
+        nv = sum(o.nv for o in batch)
+        s = N.VbdSolver(batch, dt=1 / 60, iterations=30, gravity=GRAVITY, device=local)
+        ms = statistics.mean(_timed_steps(s, 5))
+        out["batch_512_patches_30it"] = {"vertex_solves_per_s": nv * 30 / (ms * 1e-3), "ms_per_step": ms,
+                                         "vertices": nv, "colors": int(s.n_colors(-1)), "launch": list(s.launch()),
+                                         "graph": True}
+        s.close()
+    if want("implicit_euler_cloth_33x33"):
+        imp = N.ImplicitSolver([cloth], dt=1 / 60, substeps=1, gravity=GRAVITY, device=local)
+        stats = [imp.step() for _ in range(8)][3:]
+        out["implicit_euler_cloth_33x33"] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
+                                             "cg_iterations": [int(st.iterations) for st in stats],
+                                             "precision": "FP64 assembly and CG"}
         imp.close()
-    out["global_solvers_snh_beam_41x11x11"] = {"dt": "1/60 s (symplectic Euler 1e-4 s)", "precision": "FP64",
-                                               "solvers": solvers}
-    x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local)
-    ms = statistics.mean(_timed_steps(x, 5))
-    out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
-                                               "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3)}
-    x.close()
-    out["mesh_input"] = mesh_input()
-    out["topology_change"] = topology_change(local)
+    if want("implicit_euler_spring_cloth_513"):
+        imp = N.ImplicitSolver([big], dt=DT, substeps=1, gravity=GRAVITY, device=local)
+        stats = [imp.step() for _ in range(4)][1:]
+        out["implicit_euler_spring_cloth_513"] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
+                                                  "cg_iterations": [int(st.iterations) for st in stats],
+                                                  "converged": [bool(st.converged) for st in stats],
+                                                  "precision": "FP64 assembly and CG"}
+        imp.close()
+    if want("global_solvers_snh_beam_41x11x11"):
+        names = ["newton_dx", "newton_dv", "newton_robust", "baraff_witkin", "bdf2", "static_newton",
+                 "quasi_static_newton", "quasi_static_newton_robust", "symplectic_euler"]
+        solvers = {}
+        for method, name in enumerate(names):
+            dt = 1e-4 if name == "symplectic_euler" else 1 / 60
+            imp = N.ImplicitSolver([beam], dt=dt, substeps=1, gravity=GRAVITY, device=local, method=method)
+            stats = [imp.step() for _ in range(5)][2:]
+            solvers[name] = {"ms_per_step": statistics.mean(st.device_ms for st in stats),
+                             "cg_iterations": [int(st.iterations) for st in stats]}
+            imp.close()
+        out["global_solvers_snh_beam_41x11x11"] = {"dt": "1/60 s (symplectic Euler 1e-4 s)", "precision": "FP64",
+                                                   "solvers": solvers}
+    if want("xpbd_spring_cloth_513_20substeps"):
+        x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local)
+        ms = statistics.mean(_timed_steps(x, 5))
+        out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
+                                                   "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3)}
+        x.close()
+    if want("mesh_input"):
+        out["mesh_input"] = mesh_input()
+    if want("topology_change"):
+        out["topology_change"] = topology_change(local)
     return out
 
 
@@ -562,6 +576,8 @@ def main():
     ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0 = autotune)")
     ap.add_argument("--tile", type=int, default=0, help="vertices per tile of kernels 2 and 3 (0 = autotune)")
+    ap.add_argument("--config", default=None,
+                    help="run only this entry of the other configurations and print it (a profiling case)")
     ap.add_argument("--kernel", type=int, default=0,
                     help="1 = lanes per vertex, 2 = tiles, 3 = dataflow tiles (0 = autotune)")
     args = ap.parse_args()
@@ -569,6 +585,11 @@ def main():
         ap.error("--warmup must be at least 3")
     dist, rank, local, ws = _dist()
     try:
+        if args.config:
+            import torch
+            torch.cuda.set_device(local)
+            print(json.dumps(other_configs(local, only=args.config)), flush=True)
+            return 0
         if args.impl == "reference":
             return run_reference(args, dist, rank, local, ws)
         return run_gb300(args, dist, rank, local, ws)

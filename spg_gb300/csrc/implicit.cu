@@ -245,28 +245,59 @@ struct CgControl {
 
 __device__ __forceinline__ bool cg_done(const CgControl *c) { return c && *(volatile const int *)&c->done; }
 
-// Ap = A p (one thread per block row); with dots, dots[0] += p . Ap.
+// Ap = A p with LANES lanes per block row: the lanes of a row read consecutive 3x3 blocks,
+// and a shuffle reduction sums their partial products. With dots, dots[0] += p . Ap.
+// Small systems are latency bound and take 8 lanes per row; large ones are bound by the
+// part's FP64 rate (about 87 % of the FP64 pipe on the 513^2 cloth with one lane per row),
+// where the reduction's extra adds would cost more than they hide, so they take 1.
+constexpr int kSpmvLanesSmall = 8;
+constexpr int kSpmvSmallRows = 65536;
+
+template <int LANES>
 __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots,
                                      const CgControl *ctl = nullptr)
 {
     if (cg_done(ctl)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double pap = 0.0;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / LANES;
+    const int lane = t & (LANES - 1);
+    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
     if (i < nv) {
-        double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-        for (int k = __ldg(T.row_ptr + i); k < __ldg(T.row_ptr + i + 1); ++k) {
+        const int k1 = __ldg(T.row_ptr + i + 1);
+        for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
             const double *bl = T.val + size_t(k) * 9;
             const double *x = p + 3 * size_t(__ldg(T.col + k));
-            y0 += bl[0] * x[0] + bl[1] * x[1] + bl[2] * x[2];
-            y1 += bl[3] * x[0] + bl[4] * x[1] + bl[5] * x[2];
-            y2 += bl[6] * x[0] + bl[7] * x[1] + bl[8] * x[2];
+            const double x0 = x[0], x1 = x[1], x2 = x[2];
+            y0 += bl[0] * x0 + bl[1] * x1 + bl[2] * x2;
+            y1 += bl[3] * x0 + bl[4] * x1 + bl[5] * x2;
+            y2 += bl[6] * x0 + bl[7] * x1 + bl[8] * x2;
         }
+    }
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) {
+        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+    }
+    double pap = 0.0;
+    if (i < nv && lane == 0) {
         Ap[3 * i] = y0;
         Ap[3 * i + 1] = y1;
         Ap[3 * i + 2] = y2;
         pap = p[3 * i] * y0 + p[3 * i + 1] * y1 + p[3 * i + 2] * y2;
     }
     if (dots) block_reduce_add(pap, dots);
+}
+
+// One SpMV on the stream, with the lane count for the system's size.
+static void launch_spmv(const ImplicitTables &T, const double *p, double *Ap, int nv, double *dots,
+                        const CgControl *ctl, cudaStream_t st)
+{
+    if (nv < kSpmvSmallRows)
+        implicit_spmv_kernel<kSpmvLanesSmall>
+            <<<(nv * kSpmvLanesSmall + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl);
+    else
+        implicit_spmv_kernel<1><<<(nv + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl);
 }
 
 // CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z (per component).
@@ -648,7 +679,7 @@ struct ImplicitSolver {
         for (int it = 0; it < kCgChunk; ++it) {
             double *prev = it % 2 == 0 ? A : B, *cur = it % 2 == 0 ? B : A;
             cudaMemsetAsync(prev, 0, sizeof(double), stream);
-            implicit_spmv_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_p), vec(d_Ap), nv, prev, ctl);
+            launch_spmv(T, vec(d_p), vec(d_Ap), nv, prev, ctl, stream);
             cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream);
             implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
                                                                      vec(d_Ap), vec(d_dinv), n, prev, cur, ctl);
@@ -750,7 +781,7 @@ struct ImplicitSolver {
         case SPGX_IMPLICIT_BARAFF_WITKIN: {
             SPGX_CUDA(cudaMemcpyAsync(v0, v, bytes, cudaMemcpyDeviceToDevice, stream));
             assemble(x, true);
-            implicit_spmv_kernel<<<grid_of(L.nv), 256, 0, stream>>>(T, v0, vec(d_u), L.nv, nullptr);
+            launch_spmv(T, v0, vec(d_u), L.nv, nullptr, nullptr, stream);
             bw_rhs_kernel<<<g, 256, 0, stream>>>(b, f, vec(d_u), h, n);
             SPGX_TRY_STATUS(solve(1.0, h * h, t));
             lincomb_kernel<<<g, 256, 0, stream>>>(v, v0, vec(d_dx), 1.0, n);
@@ -767,7 +798,7 @@ struct ImplicitSolver {
             }
             assemble(x, true);
             bdf2_w_kernel<<<g, 256, 0, stream>>>(vec(d_w), x0, vec(d_xm1), v0, 2 * h, n);
-            implicit_spmv_kernel<<<grid_of(L.nv), 256, 0, stream>>>(T, vec(d_w), vec(d_u), L.nv, nullptr);
+            launch_spmv(T, vec(d_w), vec(d_u), L.nv, nullptr, nullptr, stream);
             bdf2_rhs_kernel<<<g, 256, 0, stream>>>(b, vec(d_mass), v0, vec(d_vm1), f, vec(d_u), h, n);
             SPGX_TRY_STATUS(solve(1.0, 4.0 / 9.0 * (h * h), t));
             lincomb_kernel<<<g, 256, 0, stream>>>(v, v0, vec(d_dx), 1.0, n);
