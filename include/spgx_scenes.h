@@ -59,6 +59,9 @@ void spgx_scene_destroy(spgx_scene *scene);
 spgx_status spgx_scene_run_gpu_vbd(spgx_scene *scene, const spgx_vbd_params *params, int32_t steps, double *x_out);
 /* Same with spg::solver::GpuXPBD. */
 spgx_status spgx_scene_run_gpu_xpbd(spgx_scene *scene, const spgx_xpbd_params *params, int32_t steps, double *x_out);
+/* Same with spg::solver::GpuImplicit for params->method (the global solvers). */
+spgx_status spgx_scene_run_gpu_implicit(spgx_scene *scene, const spgx_implicit_params *params, int32_t steps,
+                                        double *x_out);
 
 /* ---- Mesh input (spg::io::loadObj / loadMsh, spg/source/geom/io/{obj,msh}.cpp) ----------
  * spgx_load_obj: the vertices of the whole file (as float, widened to double) and the

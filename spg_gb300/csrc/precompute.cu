@@ -129,7 +129,7 @@ __device__ int tri_rest(const double *x0, const int *s, double *inv, double &are
     return area <= 0 ? kPreArea : kPreOk;
 }
 
-__global__ void precompute_kernel(int type, int n, int S, int M, int P, const int *__restrict__ stencils,
+__global__ void precompute_kernel(int type, int n, int S, int P, const int *__restrict__ stencils,
                                   const double *__restrict__ x0, const double *__restrict__ material, int mstride,
                                   double *__restrict__ params, int *__restrict__ errors)
 {
@@ -281,7 +281,6 @@ __global__ void precompute_kernel(int type, int n, int S, int M, int P, const in
     }
     default: err = -1;
     }
-    (void)M;
     errors[i] = err;
 }
 
@@ -388,8 +387,6 @@ int material_count(int type)
     }
 }
 
-int param_count_of(int type) { return spgx_param_count(type); }
-
 // One stream and device per call; buffers are released on return.
 struct DeviceScope {
     int prev = -1;
@@ -455,7 +452,7 @@ spgx_status spgx_precompute_params(int32_t type, int32_t n_stencils, const int32
                               cudaMemcpyHostToDevice, st));
     const int threads = 128;
     precompute_kernel<<<unsigned((n + threads - 1) / threads), threads, 0, st>>>(
-        type, n_stencils, S, M, P, d_st.as<int>(), d_x0.as<double>(), d_mat.as<double>(), material_stride,
+        type, n_stencils, S, P, d_st.as<int>(), d_x0.as<double>(), d_mat.as<double>(), material_stride,
         d_par.as<double>(), d_err.as<int>());
     SPGX_CUDA(cudaGetLastError());
     std::vector<int> errs(n);

@@ -100,4 +100,55 @@ private:
     bool m_hostDirty{false};
 };
 
+// The global solvers (implicitEulerNewtonDx/Dv/Robust, implicitEulerBaraffWitkin, bdf2,
+// staticNewton, quasiStaticNewton(Robust), simplecticEuler) behind one BaseSolver: the
+// method picks which reference class it replaces (spgx_implicit_method).
+class GpuImplicit : public BaseSolver {
+public:
+    explicit GpuImplicit(spgx_implicit_method method = SPGX_IMPLICIT_NEWTON_DX);
+    ~GpuImplicit() override;
+    void step() override;
+    void reset() override;
+    void requirePrecomputationUpdate() { m_dirty = true; }
+    void markHostStateDirty() { m_hostDirty = true; }
+    const spgx_step_stats &lastStats() const { return m_stats; }
+
+private:
+    void prepare();
+    spgx_implicit_params m_params{}, m_created{};
+    spgx_implicit *m_handle{nullptr};
+    spgx_step_stats m_stats{};
+    bool m_dirty{true};
+    bool m_hostDirty{false};
+};
+
+// The reference's class names over GpuImplicit.
+struct GpuImplicitEulerNewtonDx : GpuImplicit {
+    GpuImplicitEulerNewtonDx() : GpuImplicit(SPGX_IMPLICIT_NEWTON_DX) {}
+};
+struct GpuImplicitEulerNewtonDv : GpuImplicit {
+    GpuImplicitEulerNewtonDv() : GpuImplicit(SPGX_IMPLICIT_NEWTON_DV) {}
+};
+struct GpuImplicitEulerNewtonRobust : GpuImplicit {
+    GpuImplicitEulerNewtonRobust() : GpuImplicit(SPGX_IMPLICIT_NEWTON_ROBUST) {}
+};
+struct GpuImplicitEulerBaraffWitkin : GpuImplicit {
+    GpuImplicitEulerBaraffWitkin() : GpuImplicit(SPGX_IMPLICIT_BARAFF_WITKIN) {}
+};
+struct GpuBDF2 : GpuImplicit {
+    GpuBDF2() : GpuImplicit(SPGX_IMPLICIT_BDF2) {}
+};
+struct GpuStaticNewton : GpuImplicit {
+    GpuStaticNewton() : GpuImplicit(SPGX_STATIC_NEWTON) {}
+};
+struct GpuQuasiStaticNewton : GpuImplicit {
+    GpuQuasiStaticNewton() : GpuImplicit(SPGX_QUASI_STATIC_NEWTON) {}
+};
+struct GpuQuasiStaticNewtonRobust : GpuImplicit {
+    GpuQuasiStaticNewtonRobust() : GpuImplicit(SPGX_QUASI_STATIC_NEWTON_ROBUST) {}
+};
+struct GpuSimplecticEuler : GpuImplicit {
+    GpuSimplecticEuler() : GpuImplicit(SPGX_SYMPLECTIC_EULER) {}
+};
+
 }  // namespace spg::solver

@@ -219,4 +219,25 @@ spgx_status spgx_scene_run_gpu_xpbd(spgx_scene *scene, const spgx_xpbd_params *p
     SPGX_GUARD_END
 }
 
+spgx_status spgx_scene_run_gpu_implicit(spgx_scene *scene, const spgx_implicit_params *params, int32_t steps,
+                                        double *x_out)
+{
+    SPGX_GUARD_BEGIN
+    if (!scene || !params || steps < 0 || !x_out || scene->groups.empty()) {
+        spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    spg::solver::GpuImplicit solver(static_cast<spgx_implicit_method>(params->method));
+    for (const auto &g : scene->groups) solver.addObject(g);
+    solver.setDt(params->dt);
+    solver.setNumSubsteps(params->substeps);
+    solver.setGravity({params->gravity[0], params->gravity[1], params->gravity[2]});
+    for (int s = 0; s < steps; ++s) solver.step();
+    const auto &g = solver.particleGroups()[0];
+    for (int i = 0; i < g.size(); ++i)
+        for (int a = 0; a < 3; ++a) x_out[3 * i + a] = g.positions()[i][a];
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
 }  // extern "C"

@@ -234,4 +234,71 @@ void GpuXPBD::reset()
     m_dirty = true;
 }
 
+GpuImplicit::GpuImplicit(spgx_implicit_method method)
+{
+    spgx_implicit_params_default(&m_params);
+    m_params.method = method;
+}
+
+GpuImplicit::~GpuImplicit() { spgx_implicit_destroy(m_handle); }
+
+// First step or after a topology change: the system pattern is built from the current groups.
+void GpuImplicit::prepare()
+{
+    spgx_implicit_destroy(m_handle);
+    m_handle = nullptr;
+    gpu::PackedScene scene;
+    gpu::pack(m_objects, scene);
+    check(spgx_implicit_create(&scene.desc, &m_params, &m_handle));
+    m_dirty = false;
+    m_hostDirty = false;
+}
+
+void GpuImplicit::step()
+{
+    m_params.dt = m_dtStep;
+    m_params.substeps = m_nsubsteps;
+    for (int a = 0; a < 3; ++a) m_params.gravity[a] = m_gravity[a];
+    // dt, substeps and gravity are fixed at creation: a change rebuilds the handle from the
+    // groups (which hold the state of the last step).
+    const bool changed = m_params.dt != m_created.dt || m_params.substeps != m_created.substeps ||
+                         m_params.gravity[0] != m_created.gravity[0] || m_params.gravity[1] != m_created.gravity[1] ||
+                         m_params.gravity[2] != m_created.gravity[2];
+    if (m_dirty || !m_handle || changed) {
+        prepare();
+        m_created = m_params;
+    }
+    if (m_hostDirty) {
+        for (int o = 0; o < numSimObjects(); ++o) {
+            const auto &g = m_objects[o];
+            std::vector<double> x(3 * g.size()), v(3 * g.size());
+            for (int i = 0; i < g.size(); ++i)
+                for (int a = 0; a < 3; ++a) {
+                    x[3 * i + a] = g.positions()[i][a];
+                    v[3 * i + a] = g.velocities()[i][a];
+                }
+            check(spgx_implicit_set_state(m_handle, o, x.data(), v.data()));
+        }
+        m_hostDirty = false;
+    }
+    check(spgx_implicit_step(m_handle, &m_stats));
+    for (int o = 0; o < numSimObjects(); ++o) {
+        auto &g = m_objects[o];
+        std::vector<double> x(3 * g.size()), v(3 * g.size());
+        check(spgx_implicit_get_state(m_handle, o, x.data(), v.data()));
+        for (int i = 0; i < g.size(); ++i) {
+            g.positions()[i] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+            g.velocities()[i] = {v[3 * i], v[3 * i + 1], v[3 * i + 2]};
+        }
+    }
+}
+
+void GpuImplicit::reset()
+{
+    BaseSolver::reset();
+    spgx_implicit_destroy(m_handle);  // also restarts the step control and BDF2's history
+    m_handle = nullptr;
+    m_dirty = true;
+}
+
 }  // namespace spg::solver

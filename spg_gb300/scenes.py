@@ -54,6 +54,7 @@ def _lib():
         L.spgx_scene_destroy.argtypes = [vp]
         L.spgx_scene_run_gpu_vbd.argtypes = [vp, C.POINTER(N.VbdParams), i32, C.POINTER(f64)]
         L.spgx_scene_run_gpu_xpbd.argtypes = [vp, C.POINTER(N.XpbdParams), i32, C.POINTER(f64)]
+        L.spgx_scene_run_gpu_implicit.argtypes = [vp, C.POINTER(N.ImplicitParams), i32, C.POINTER(f64)]
         pi = C.POINTER(i32)
         L.spgx_scene_triangle_mesh.argtypes = [C.POINTER(f64), i32, pi, i32, f64, f64, f64, f64, i32, pi,
                                                C.POINTER(vp)]
@@ -109,6 +110,17 @@ class Scene:
         p = N.vbd_params(**params)
         out = np.zeros((self.objects[0].nv, 3))
         N.check(_lib().spgx_scene_run_gpu_vbd(self.h, C.byref(p), steps, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def run_gpu_implicit(self, steps, dt, substeps, gravity, method):
+        """Runs spg::solver::GpuImplicit (the given global solver) and returns object 0's positions."""
+        p = N.ImplicitParams()
+        N.lib().spgx_implicit_params_default(C.byref(p))
+        p.dt, p.substeps, p.method = dt, substeps, method
+        p.gravity = (C.c_double * 3)(*gravity)
+        out = np.zeros((self.objects[0].nv, 3))
+        N.check(_lib().spgx_scene_run_gpu_implicit(self.h, C.byref(p), steps,
+                                                   out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
 
     def run_gpu_xpbd(self, steps, dt, substeps, gravity):
