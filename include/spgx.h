@@ -428,6 +428,10 @@ spgx_status spgx_implicit_step(spgx_implicit *h, spgx_step_stats *stats);
 spgx_status spgx_implicit_get_state(spgx_implicit *h, int32_t object, double *x, double *v);
 spgx_status spgx_implicit_set_state(spgx_implicit *h, int32_t object, const double *x, const double *v);
 spgx_status spgx_implicit_reset(spgx_implicit *h);
+/* New dt, substeps, gravity and CG settings for the following steps (BaseSolver::setDt etc.
+ * between steps). The robust methods' step size and BDF2's history carry over, as in the
+ * reference. method and device must equal the created ones (else SPGX_ERR_INVALID_ARG). */
+spgx_status spgx_implicit_set_params(spgx_implicit *h, const spgx_implicit_params *params);
 /* The robust methods' current substep (m_currentDt; -1 before the first step). */
 spgx_status spgx_implicit_get_step_size(spgx_implicit *h, double *dt);
 

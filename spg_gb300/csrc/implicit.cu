@@ -531,6 +531,19 @@ struct ImplicitSolver {
         return SPGX_OK;
     }
 
+    // BaseSolver::setDt / setNumSubsteps / setGravity between steps: the next step reads the
+    // new values. The step size and BDF2's history carry over; method and device are fixed.
+    spgx_status set_params(const spgx_implicit_params *p)
+    {
+        SPGX_TRY_STATUS(check_params(p));
+        if (p->method != P.method || p->device != P.device) {
+            set_error("method and device are fixed when the solver is created");
+            return SPGX_ERR_INVALID_ARG;
+        }
+        P = *p;
+        return SPGX_OK;
+    }
+
     int n3() const { return 3 * L.nv; }
     double *vec(DevBuf &b) { return b.as<double>(); }
 
@@ -1140,6 +1153,14 @@ spgx_status spgx_implicit_reset(spgx_implicit *h)
     SPGX_GUARD_BEGIN
     SPGX_IHANDLE(h);
     return h->s->reset();
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_implicit_set_params(spgx_implicit *h, const spgx_implicit_params *params)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_IHANDLE(h);
+    return h->s->set_params(params);
     SPGX_GUARD_END
 }
 

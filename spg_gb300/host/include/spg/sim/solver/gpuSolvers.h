@@ -115,7 +115,7 @@ public:
 
 private:
     void prepare();
-    spgx_implicit_params m_params{}, m_created{};
+    spgx_implicit_params m_params{};
     spgx_implicit *m_handle{nullptr};
     spgx_step_stats m_stats{};
     bool m_dirty{true};

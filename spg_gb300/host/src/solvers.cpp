@@ -259,14 +259,12 @@ void GpuImplicit::step()
     m_params.dt = m_dtStep;
     m_params.substeps = m_nsubsteps;
     for (int a = 0; a < 3; ++a) m_params.gravity[a] = m_gravity[a];
-    // dt, substeps and gravity are fixed at creation: a change rebuilds the handle from the
-    // groups (which hold the state of the last step).
-    const bool changed = m_params.dt != m_created.dt || m_params.substeps != m_created.substeps ||
-                         m_params.gravity[0] != m_created.gravity[0] || m_params.gravity[1] != m_created.gravity[1] ||
-                         m_params.gravity[2] != m_created.gravity[2];
-    if (m_dirty || !m_handle || changed) {
+    if (m_dirty || !m_handle) {
         prepare();
-        m_created = m_params;
+    } else {
+        // setDt / setNumSubsteps / setGravity between steps: the handle keeps its step control
+        // and BDF2 history, as the reference's solver object does.
+        check(spgx_implicit_set_params(m_handle, &m_params));
     }
     if (m_hostDirty) {
         for (int o = 0; o < numSimObjects(); ++o) {

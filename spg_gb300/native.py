@@ -150,6 +150,7 @@ def lib():
         L.spgx_implicit_set_state.argtypes = [vp, i32, dp, dp]
         L.spgx_implicit_reset.argtypes = [vp]
         L.spgx_implicit_get_step_size.argtypes = [vp, dp]
+        L.spgx_implicit_set_params.argtypes = [vp, C.POINTER(ImplicitParams)]
         _lib = L
     return _lib
 
@@ -442,6 +443,18 @@ class ImplicitSolver:
 
     def reset(self):
         check(lib().spgx_implicit_reset(self.h))
+
+    def set_params(self, dt=None, substeps=None, gravity=None):
+        """Changes dt / substeps / gravity for the following steps; the step control and
+        BDF2's history carry over."""
+        p = self.params
+        if dt is not None:
+            p.dt = dt
+        if substeps is not None:
+            p.substeps = substeps
+        if gravity is not None:
+            p.gravity = (C.c_double * 3)(*gravity)
+        check(lib().spgx_implicit_set_params(self.h, C.byref(p)))
 
     def step_size(self) -> float:
         """The robust methods' current substep (-1 before the first step)."""

@@ -3,6 +3,8 @@ FP64 oracle's conjugate-gradient restatement against a direct solve (CPU), and t
 solver against the oracle on scenes with every energy type (GB300). Continuum springs run on
 a 3D truss: on a flat cloth at rest the implicit step is nearly singular out of plane, and a
 1e-9 m perturbation grows to millimetres in one step in the FP64 oracle itself."""
+import ctypes as C
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -121,6 +123,35 @@ def test_methods_match_oracle(method, name):
     if method in (IR.NEWTON_ROBUST, IR.QUASI_STATIC_NEWTON_ROBUST):
         assert failed == ref.failed_substeps
         assert gpu.step_size() == ref.current_dt
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method,name", [(IR.NEWTON_ROBUST, "stvk_cloth"), (IR.BDF2, "snh_beam")])
+def test_changing_dt_between_steps_keeps_history(method, name):
+    """setDt between steps: the robust step control and BDF2's previous state carry over
+    (implicitEulerNewtonRobust.cpp:37-40 clamps m_currentDt to the new maximum; bdf2.cpp:66-67
+    keeps m_xMinusOne / m_vMinusOne). Halving dt after five steps must match the oracle doing the same."""
+    N = pytest.importorskip("spg_gb300.native")
+    obj = _scenes()[name].copy()
+    gpu = N.ImplicitSolver([obj], dt=1 / 60, substeps=1, gravity=scenes.GRAVITY, method=method)
+    ref = IR.ImplicitSolver(obj, 1 / 60, 1, scenes.GRAVITY, method)
+    for k in range(10):
+        if k == 5:
+            gpu.set_params(dt=1 / 120)
+            ref.dt = 1 / 120
+        gpu.step()
+        ref.step()
+    xg, _ = gpu.state(0)
+    xr, _ = ref.state()
+    err = float(np.abs(xg - xr).max())
+    moved = float(np.abs(xr - obj.x).max())
+    assert err <= 1e-4 * float(np.ptp(obj.x0, axis=0).max()) and err <= 1e-3 * moved
+    if method == IR.NEWTON_ROBUST:
+        assert gpu.step_size() == ref.current_dt
+    p = N.ImplicitParams()
+    C.memmove(C.byref(p), C.byref(gpu.params), C.sizeof(p))
+    p.method = IR.NEWTON_DX
+    assert N.STATUS[N.lib().spgx_implicit_set_params(gpu.h, C.byref(p))] == "INVALID_ARG"
 
 
 @pytest.mark.gpu
