@@ -63,13 +63,16 @@ SPGX_HD Vec3<T> cross(Vec3<T> a, Vec3<T> b)
 
 SPGX_HD float sq_root(float a) { return sqrtf(a); }
 SPGX_HD double sq_root(double a) { return sqrt(a); }
-// 1/x and 1/sqrt(x). On the device the FP32 forms use the correctly rounded reciprocal and the
-// hardware reciprocal square root (about 2 ulp), which shortens the dependency chains of the
-// element blocks; the CPU instantiations keep plain division.
+// 1/x and 1/sqrt(x). On the device the FP32 forms use the hardware's approximate reciprocal
+// (PTX rcp.approx.f32, within 1 ulp) and reciprocal square root (about 2 ulp): single
+// instructions instead of rounding sequences in the element blocks' dependency chains. The CPU
+// instantiations keep plain division.
 SPGX_HD float recip(float a)
 {
 #if defined(__CUDA_ARCH__)
-    return __frcp_rn(a);
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
 #else
     return 1.f / a;
 #endif
@@ -84,7 +87,36 @@ SPGX_HD float rsqrt_of(float a)
 #endif
 }
 SPGX_HD double rsqrt_of(double a) { return 1.0 / sqrt(a); }
-SPGX_HD float arctan2(float y, float x) { return atan2f(y, x); }
+// FP32 atan2 on the device: t = min(|x|, |y|) / max(|x|, |y|) in [0, 1], atan(t) = t P(t^2)
+// with P the degree-8 minimax polynomial in relative error (Remez exchange; atan_poly_fit.py
+// beside this file fits it: 2 ulp in FP32 Horner form), then the octant is restored:
+// pi/2 - r when |y| > |x|, pi - r when x is negative (or -0), and the sign of y. Finite
+// arguments only, as the hinge angles of non-degenerate triangles are; atan2(+-0, +0) = +-0
+// and atan2(+-0, -0) = +-pi as in C.
+SPGX_HD float arctan2(float y, float x)
+{
+#if defined(__CUDA_ARCH__)
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float hi = fmaxf(ax, ay), lo = fminf(ax, ay);
+    const float t = hi > 0.f ? lo * recip(hi) : 0.f;
+    const float s = t * t;
+    float p = 0.002849889686331153f;
+    p = fmaf(p, s, -0.016068629920482635f);
+    p = fmaf(p, s, 0.04269152134656906f);
+    p = fmaf(p, s, -0.07504294812679291f);
+    p = fmaf(p, s, 0.10640934109687805f);
+    p = fmaf(p, s, -0.14203643798828125f);
+    p = fmaf(p, s, 0.1999261975288391f);
+    p = fmaf(p, s, -0.3333307206630707f);
+    p = fmaf(p, s, 1.0f);
+    float r = t * p;
+    if (ay > ax) r = 1.5707963267948966f - r;
+    if (signbit(x)) r = 3.141592653589793f - r;
+    return copysignf(r, y);
+#else
+    return atan2f(y, x);
+#endif
+}
 SPGX_HD double arctan2(double y, double x) { return atan2(y, x); }
 
 template <typename T>
