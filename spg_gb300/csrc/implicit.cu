@@ -58,7 +58,26 @@ struct ImplicitTables {
     const int *col;      // BSR block columns
     double *val;         // BSR values, 9 per block (row-major)
     const int *diag;     // per vertex: position of its diagonal block
+    float2 *val2;        // the CG's system matrix in double-float form (split_df), 9 per block
+    int *wide;           // set when the CG's matrix or direction leaves the double-float range
 };
+
+// Double-float form of an FP64 value: a = hi + lo with hi = fl32(a) and lo = fl32(a - hi),
+// 48 significant bits. GB300 runs FP64 at about 1/64 of its FP32 rate, so the CG's products
+// (the solve's only O(nnz) arithmetic) run on the FP32 pipes in this form. A value above 2^60
+// in magnitude, or not finite, reports out of range: the SpMV then falls back to FP64.
+__device__ __forceinline__ float2 split_df(double a, bool &out_of_range)
+{
+    out_of_range = !(fabs(a) <= 0x1p60);
+    const float hi = __double2float_rn(a);
+    return make_float2(hi, __double2float_rn(a - double(hi)));
+}
+
+// Sets *wide once per warp if any lane of the warp saw an out-of-range value.
+__device__ __forceinline__ void flag_wide(bool bad, int *wide)
+{
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(wide, 1);
+}
 
 // Vectors over the vertices: 3 doubles per vertex.
 __device__ __forceinline__ void atomic_block(double *val, int blk, const double H[9])
@@ -73,6 +92,156 @@ __device__ __forceinline__ void atomic_force(double *f, int v, double gx, double
     atomicAdd(f + 3 * v, -gx);
     atomicAdd(f + 3 * v + 1, -gy);
     atomicAdd(f + 3 * v + 2, -gz);
+}
+
+// First-order forward mode with the three coordinates of one vertex as tangents: the
+// Hessian of an energy whose gradient has a closed form is the derivative of that gradient.
+struct D3 {
+    double v, d[3];
+};
+__device__ __forceinline__ D3 operator+(D3 a, D3 b)
+{
+    return {a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2]}};
+}
+__device__ __forceinline__ D3 operator-(D3 a, D3 b)
+{
+    return {a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2]}};
+}
+__device__ __forceinline__ D3 operator-(D3 a) { return {-a.v, {-a.d[0], -a.d[1], -a.d[2]}}; }
+__device__ __forceinline__ D3 operator*(D3 a, D3 b)
+{
+    return {a.v * b.v, {a.d[0] * b.v + a.v * b.d[0], a.d[1] * b.v + a.v * b.d[1], a.d[2] * b.v + a.v * b.d[2]}};
+}
+__device__ __forceinline__ D3 recip(D3 a)
+{
+    const double r = 1.0 / a.v, s = -r * r;
+    return {r, {s * a.d[0], s * a.d[1], s * a.d[2]}};
+}
+__device__ __forceinline__ D3 sq_root(D3 a)
+{
+    const double r = sqrt(a.v), s = 0.5 / r;
+    return {r, {s * a.d[0], s * a.d[1], s * a.d[2]}};
+}
+
+template <typename T>
+__device__ __forceinline__ T comp(const Vec3<T> &v, int r)
+{
+    return r == 0 ? v.x : (r == 1 ? v.y : v.z);
+}
+
+// Gradient of the dihedral angle of DiscreteBendingEnergy (discreteBendingEnergy.cpp; hinge
+// x0-x1, flaps x2 and x3) with respect to x1, x2 and x3, from e = x1 - x0, a = x2 - x0,
+// b = x3 - x0, Na = e x a, Nb = e x b:
+//   dtheta/dx1 = (a.e) Na / (|e| |Na|^2) - (b.e) Nb / (|e| |Nb|^2),
+//   dtheta/dx2 = -|e| Na / |Na|^2,   dtheta/dx3 = |e| Nb / |Nb|^2,
+// and dtheta/dx0 = -(the sum of the three).
+template <typename T>
+__device__ __forceinline__ void dihedral_gradient(Vec3<T> e, Vec3<T> a, Vec3<T> b, Vec3<T> g[3])
+{
+    const Vec3<T> Na = cross(e, a), Nb = cross(e, b);
+    const T L = sq_root(dot(e, e));
+    const T iL = recip(L);
+    const T ina = recip(dot(Na, Na)), inb = recip(dot(Nb, Nb));
+    g[0] = (dot(a, e) * iL * ina) * Na - (dot(b, e) * iL * inb) * Nb;
+    g[1] = (-(L * ina)) * Na;
+    g[2] = (L * inb) * Nb;
+}
+
+// DiscreteBendingEnergy, E = 1/2 k (theta - theta0)^2 (prm = [theta0, k]): gradient
+// k C grad theta and Hessian k (grad theta grad theta^T + C hess theta), C = theta - theta0,
+// theta = atan2(-|e| Na.b, -Na.Nb) (the reference's atan2 of the normals, simplified).
+// hess theta is the forward-mode derivative of the closed-form gradient, one seeded vertex
+// (x1, x2, x3) at a time; column x0 follows from translation invariance.
+template <bool kHess>
+__device__ void assemble_bending(const ImplicitTables &T, const double *__restrict__ x, double *force, int e,
+                                 int4 ix, const double *prm)
+{
+    const int iv[4] = {ix.x, ix.y, ix.z, ix.w};
+    const int *eb = T.eblk + size_t(e) * 16;
+    const double *x0 = x + 3 * size_t(iv[0]);
+    Vec3<double> p[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const double *xj = x + 3 * size_t(iv[j + 1]);
+        p[j] = mk(xj[0] - x0[0], xj[1] - x0[1], xj[2] - x0[2]);
+    }
+    const Vec3<double> Na = cross(p[0], p[1]), Nb = cross(p[0], p[2]);
+    const double th = atan2(-sqrt(dot(p[0], p[0])) * dot(Na, p[2]), -dot(Na, Nb));
+    const double k = prm[1], C = th - prm[0];
+    Vec3<double> g[4];
+    dihedral_gradient<double>(p[0], p[1], p[2], g + 1);
+    g[0] = mk(-(g[1].x + g[2].x + g[3].x), -(g[1].y + g[2].y + g[3].y), -(g[1].z + g[2].z + g[3].z));
+#pragma unroll
+    for (int a = 0; a < 4; ++a) atomic_force(force, iv[a], k * C * g[a].x, k * C * g[a].y, k * C * g[a].z);
+    if (!kHess) return;
+    double D00[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) D00[q] = 0.0;
+#pragma unroll
+    for (int sv = 1; sv < 4; ++sv) {
+        Vec3<D3> q[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const double t = j + 1 == sv ? 1.0 : 0.0;
+            q[j] = mk(D3{p[j].x, {t, 0.0, 0.0}}, D3{p[j].y, {0.0, t, 0.0}}, D3{p[j].z, {0.0, 0.0, t}});
+        }
+        Vec3<D3> dg[3];
+        dihedral_gradient<D3>(q[0], q[1], q[2], dg);
+        // J_a[r][c] = d g_a[r] / d x_sv[c] for a = 1..3; a = 0 is minus their sum.
+        double H[9], Ht[9];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const double J = a == 0 ? -(comp(dg[0], r).d[c] + comp(dg[1], r).d[c] + comp(dg[2], r).d[c])
+                                            : comp(dg[a - 1], r).d[c];
+                    if (a == 0) D00[3 * r + c] -= J;
+                    H[3 * r + c] = k * (comp(g[a], r) * comp(g[sv], c) + C * J);
+                    Ht[3 * c + r] = H[3 * r + c];
+                }
+            atomic_block(T.val, eb[a * 4 + sv], H);
+            if (a == 0) atomic_block(T.val, eb[sv * 4], Ht);
+        }
+    }
+    double H[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) H[3 * r + c] = k * (comp(g[0], r) * comp(g[0], c) + C * D00[3 * r + c]);
+    atomic_block(T.val, eb[0], H);
+}
+
+// SpringEnergy, E = 1/2 k (|x0 - x1| - L0)^2 (prm = [L0, k]): with d = x0 - x1, l = |d|,
+// grad_0 = k (l - L0) d / l = -grad_1 and H_00 = H_11 = -H_01 = -H_10
+// = k ((1 - L0 / l) I + L0 d d^T / l^3).
+template <bool kHess>
+__device__ void assemble_spring(const ImplicitTables &T, const double *__restrict__ x, double *force, int e, int4 ix,
+                                const double *prm)
+{
+    const double *xa = x + 3 * size_t(ix.x), *xb = x + 3 * size_t(ix.y);
+    const double d[3] = {xa[0] - xb[0], xa[1] - xb[1], xa[2] - xb[2]};
+    const double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double L0 = prm[0], k = prm[1], il = 1.0 / l;
+    const double s = k * (l - L0) * il;
+    atomic_force(force, ix.x, s * d[0], s * d[1], s * d[2]);
+    atomic_force(force, ix.y, -s * d[0], -s * d[1], -s * d[2]);
+    if (!kHess) return;
+    const double dg = k * (1.0 - L0 * il), o = k * L0 * il * il * il;
+    double H[9], Hn[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            H[3 * r + c] = (r == c ? dg : 0.0) + o * d[r] * d[c];
+            Hn[3 * r + c] = -H[3 * r + c];
+        }
+    const int *eb = T.eblk + size_t(e) * 16;
+    atomic_block(T.val, eb[0], H);
+    atomic_block(T.val, eb[1], Hn);
+    atomic_block(T.val, eb[2], Hn);
+    atomic_block(T.val, eb[3], H);
 }
 
 // Gradient and Hessian blocks of one element at the positions x (FP64, 3 per vertex), added to
@@ -189,9 +358,19 @@ __global__ void __launch_bounds__(128) implicit_assemble_kernel(ImplicitTables T
         }
         return;
     }
-    case 2: assemble_element<2, kHess>(T, x, force, e, ix, info); break;
+    case 2:
+        if (info.x == SPGX_ENERGY_SPRING)
+            assemble_spring<kHess>(T, x, force, e, ix, prm);
+        else
+            assemble_element<2, kHess>(T, x, force, e, ix, info);
+        break;
     case 3: assemble_element<3, kHess>(T, x, force, e, ix, info); break;
-    default: assemble_element<4, kHess>(T, x, force, e, ix, info); break;
+    default:
+        if (info.x == SPGX_ENERGY_DISCRETE_BENDING)
+            assemble_bending<kHess>(T, x, force, e, ix, prm);
+        else
+            assemble_element<4, kHess>(T, x, force, e, ix, info);
+        break;
     }
 }
 
@@ -216,19 +395,51 @@ __global__ void implicit_lhs_kernel(ImplicitTables T, const double *mass, int nv
     dinv[3 * i + 2] = b[8] != 0.0 ? 1.0 / b[8] : 1.0;
 }
 
-__device__ __forceinline__ void block_reduce_add(double v, double *out)
+// val2 = split_df(val) over all 9 nnzb values. A nonzero diagonal below 2^-60 in magnitude
+// (a row whose scale nears FP32's underflow) also selects the FP64 SpMV.
+__global__ void implicit_split_kernel(ImplicitTables T, size_t n_values, int nv)
 {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __shared__ double part[32];
+    bool bad = false;
+    for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n_values; k += size_t(gridDim.x) * blockDim.x) {
+        bool o;
+        T.val2[k] = split_df(T.val[k], o);
+        bad |= o;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
+        const double *d = T.val + size_t(T.diag[i]) * 9;
+        for (int q = 0; q < 9; q += 4)
+            if (d[q] != 0.0 && fabs(d[q]) < 0x1p-60) bad = true;
+    }
+    flag_wide(bad, T.wide);
+}
+
+// Block-wide FP64 sums of a and b into *oa and *ob (one atomic each per block; ob may be
+// NULL). Each kernel calls this once: the shared partials are not reused within a launch.
+__device__ __forceinline__ void block_reduce_add2(double a, double b, double *oa, double *ob)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    __shared__ double part[2][32];
     const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) part[w] = v;
+    if ((threadIdx.x & 31) == 0) {
+        part[0][w] = a;
+        part[1][w] = b;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int k = 0; k < (blockDim.x + 31) / 32; ++k) s += part[k];
-        atomicAdd(out, s);
+        double sa = 0.0, sb = 0.0;
+        for (int k = 0; k < (blockDim.x + 31) / 32; ++k) {
+            sa += part[0][k];
+            sb += part[1][k];
+        }
+        atomicAdd(oa, sa);
+        if (ob) atomicAdd(ob, sb);
     }
 }
+
+__device__ __forceinline__ void block_reduce_add(double v, double *out) { block_reduce_add2(v, 0.0, out, nullptr); }
 
 // Device-side control of one CG solve: the iteration loop runs as captured graphs of several
 // iterations with no host round trip per iteration; once done is set every later kernel of
@@ -247,37 +458,99 @@ __device__ __forceinline__ bool cg_done(const CgControl *c) { return c && *(vola
 
 // Ap = A p with LANES lanes per block row: the lanes of a row read consecutive 3x3 blocks,
 // and a shuffle reduction sums their partial products. With dots, dots[0] += p . Ap.
-// Small systems are latency bound and take 8 lanes per row; large ones are bound by the
-// part's FP64 rate (about 87 % of the FP64 pipe on the 513^2 cloth with one lane per row),
-// where the reduction's extra adds would cost more than they hide, so they take 1.
+// Small systems are latency bound and take 8 lanes per row. Large ones take 4 in
+// double-float (coalesced block reads; the 513^2 cloth step was 2 % faster than with 1 lane
+// and 4 % faster than with 8) and 1 in FP64, where the FP64 pipe binds and the reduction's
+// extra adds would cost more than they hide.
 constexpr int kSpmvLanesSmall = 8;
+constexpr int kSpmvLanesLarge = 4;
 constexpr int kSpmvSmallRows = 65536;
+constexpr int kSplitBlocks = 152 * 8;  // grid-stride split of the system matrix
 
+// s += a x in double-float: the head product's rounding error comes back exactly from an
+// FMA, the heads are summed by Knuth's two-sum, and the tails and errors gather in sl.
+// The _rn intrinsics keep the compiler from contracting the products into the sums.
+__device__ __forceinline__ void df_fma(float &sh, float &sl, float2 a, float2 x)
+{
+    const float ph = __fmul_rn(a.x, x.x);
+    const float pl = fmaf(a.x, x.y, fmaf(a.y, x.x, fmaf(a.x, x.x, -ph)));
+    const float s = __fadd_rn(sh, ph);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(e, pl));
+}
+
+// (sh, sl) += (bh, bl) in double-float (two-sum of the heads).
+__device__ __forceinline__ void df_add(float &sh, float &sl, float bh, float bl)
+{
+    const float s = __fadd_rn(sh, bh);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(e, bl));
+}
+
+// With p2 (the CG, when *T.wide is clear) the products and the lane reduction run in
+// double-float on T.val2 and p2, and lane 0 rounds the sums to FP64; otherwise everything runs
+// in FP64 on T.val and p. The choice is the same for the whole grid.
 template <int LANES>
 __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots,
-                                     const CgControl *ctl = nullptr)
+                                     const CgControl *ctl = nullptr, const float2 *__restrict__ p2 = nullptr)
 {
     if (cg_done(ctl)) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / LANES;
     const int lane = t & (LANES - 1);
     double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-    if (i < nv) {
-        const int k1 = __ldg(T.row_ptr + i + 1);
-        for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
-            const double *bl = T.val + size_t(k) * 9;
-            const double *x = p + 3 * size_t(__ldg(T.col + k));
-            const double x0 = x[0], x1 = x[1], x2 = x[2];
-            y0 += bl[0] * x0 + bl[1] * x1 + bl[2] * x2;
-            y1 += bl[3] * x0 + bl[4] * x1 + bl[5] * x2;
-            y2 += bl[6] * x0 + bl[7] * x1 + bl[8] * x2;
+    if (p2 && !*(volatile const int *)T.wide) {
+        float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+        if (i < nv) {
+            const int k1 = __ldg(T.row_ptr + i + 1);
+            for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
+                const float2 *bl = T.val2 + size_t(k) * 9;
+                const float2 *x = p2 + 3 * size_t(__ldg(T.col + k));
+                const float2 x0 = x[0], x1 = x[1], x2 = x[2];
+                df_fma(h0, l0, bl[0], x0);
+                df_fma(h0, l0, bl[1], x1);
+                df_fma(h0, l0, bl[2], x2);
+                df_fma(h1, l1, bl[3], x0);
+                df_fma(h1, l1, bl[4], x1);
+                df_fma(h1, l1, bl[5], x2);
+                df_fma(h2, l2, bl[6], x0);
+                df_fma(h2, l2, bl[7], x1);
+                df_fma(h2, l2, bl[8], x2);
+            }
         }
-    }
 #pragma unroll
-    for (int o = LANES / 2; o > 0; o >>= 1) {
-        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
-        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
-        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+        for (int o = LANES / 2; o > 0; o >>= 1) {
+            df_add(h0, l0, __shfl_xor_sync(0xffffffffu, h0, o), __shfl_xor_sync(0xffffffffu, l0, o));
+            df_add(h1, l1, __shfl_xor_sync(0xffffffffu, h1, o), __shfl_xor_sync(0xffffffffu, l1, o));
+            df_add(h2, l2, __shfl_xor_sync(0xffffffffu, h2, o), __shfl_xor_sync(0xffffffffu, l2, o));
+        }
+        if (lane == 0) {
+            y0 = double(h0) + double(l0);
+            y1 = double(h1) + double(l1);
+            y2 = double(h2) + double(l2);
+        }
+    } else {
+        if (i < nv) {
+            const int k1 = __ldg(T.row_ptr + i + 1);
+            for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
+                const double *bl = T.val + size_t(k) * 9;
+                const double *x = p + 3 * size_t(__ldg(T.col + k));
+                const double x0 = x[0], x1 = x[1], x2 = x[2];
+                y0 += bl[0] * x0 + bl[1] * x1 + bl[2] * x2;
+                y1 += bl[3] * x0 + bl[4] * x1 + bl[5] * x2;
+                y2 += bl[6] * x0 + bl[7] * x1 + bl[8] * x2;
+            }
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) {
+            y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+            y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+            y2 += __shfl_xor_sync(0xffffffffu, y2, o);
+        }
     }
     double pap = 0.0;
     if (i < nv && lane == 0) {
@@ -291,34 +564,39 @@ __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict_
 
 // One SpMV on the stream, with the lane count for the system's size.
 static void launch_spmv(const ImplicitTables &T, const double *p, double *Ap, int nv, double *dots,
-                        const CgControl *ctl, cudaStream_t st)
+                        const CgControl *ctl, cudaStream_t st, const float2 *p2 = nullptr)
 {
     if (nv < kSpmvSmallRows)
         implicit_spmv_kernel<kSpmvLanesSmall>
-            <<<(nv * kSpmvLanesSmall + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl);
+            <<<(nv * kSpmvLanesSmall + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl, p2);
+    else if (p2)
+        implicit_spmv_kernel<kSpmvLanesLarge>
+            <<<(nv * kSpmvLanesLarge + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl, p2);
     else
-        implicit_spmv_kernel<1><<<(nv + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl);
+        implicit_spmv_kernel<1><<<(nv + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl, p2);
 }
 
 // CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z (per component).
 __global__ void implicit_cg_init_kernel(const double *b, const double *dinv, double *x, double *r, double *z,
-                                       double *p, int n, double *dots)
+                                       double *p, float2 *p2, int *wide, int n, double *dots)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0, rz = 0.0;
-    if (i < n) {
+    bool bad = false;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double ri = b[i], zi = ri * dinv[i];
         x[i] = 0.0;
         r[i] = ri;
         z[i] = zi;
         p[i] = zi;
-        rr = ri * ri;
-        rz = ri * zi;
+        bool o;
+        p2[i] = split_df(zi, o);
+        bad |= o;
+        rr += ri * ri;
+        rz += ri * zi;
     }
-    block_reduce_add(rr, dots + 1);
-    block_reduce_add(rz, dots + 2);
+    flag_wide(bad, wide);
+    block_reduce_add2(rr, rz, dots + 1, dots + 2);
 }
-
 // Eigen's start: nothing to do for b = 0; otherwise iterate while |r|^2 >= tol^2 |b|^2.
 __global__ void implicit_cg_control_kernel(CgControl *c, const double *dots, double tol, int max_its)
 {
@@ -338,27 +616,27 @@ __global__ void implicit_cg_update_kernel(double *x, double *r, double *z, const
 {
     if (cg_done(ctl)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) ++ctl->its;  // read by the direction kernel
-    const double alpha = prev[2] / prev[0];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_alpha;
+    if (threadIdx.x == 0) s_alpha = prev[2] / prev[0];
+    __syncthreads();
+    const double alpha = s_alpha;
     double rr = 0.0, rz = 0.0;
-    if (i < n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
         const double ri = r[i] - alpha * Ap[i];
         r[i] = ri;
         const double zi = ri * dinv[i];
         z[i] = zi;
-        rr = ri * ri;
-        rz = ri * zi;
+        rr += ri * ri;
+        rz += ri * zi;
     }
-    block_reduce_add(rr, dots + 1);
-    block_reduce_add(rz, dots + 2);
+    block_reduce_add2(rr, rz, dots + 1, dots + 2);
 }
-
 // The iteration's stopping test (Eigen: |r|^2 < thr2 after the update, or the iteration
 // limit), then p = z + beta p with beta = rz_new / rz_old. Every block takes the same
 // decision: its inputs were written by earlier kernels.
-__global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, const double *prev, const double *cur,
-                                            CgControl *ctl)
+__global__ void implicit_cg_direction_kernel(double *p, float2 *p2, int *wide, const double *z, int n,
+                                            const double *prev, const double *cur, CgControl *ctl)
 {
     if (cg_done(ctl)) return;
     const double rr = cur[1];
@@ -370,10 +648,19 @@ __global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, 
         }
     }
     if (stop) return;
-    const double beta = cur[2] / prev[2];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    p[i] = z[i] + beta * p[i];
+    __shared__ double s_beta;
+    if (threadIdx.x == 0) s_beta = cur[2] / prev[2];
+    __syncthreads();
+    const double beta = s_beta;
+    bool bad = false;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double pi = z[i] + beta * p[i];
+        p[i] = pi;
+        bool o;
+        p2[i] = split_df(pi, o);
+        bad |= o;
+    }
+    flag_wide(bad, wide);
 }
 
 // ---- vector steps of the methods (n = 3 V degrees of freedom; mass per vertex) ------------
@@ -490,6 +777,9 @@ __global__ void symplectic_kernel(double *v, const double *f, const double *mass
 }
 
 static int grid_of(int n, int t = 256) { return (n + t - 1) / t; }
+// The CG's vector kernels loop over several entries per thread, so their FP64 block
+// reductions (a shuffle tree per thread) are paid once per few entries: 8 blocks of 256 per SM.
+static int cg_grid(int n) { return std::max(1, std::min(grid_of(n), 152 * 8)); }
 
 struct ImplicitSolver {
     SceneLayout L;
@@ -500,6 +790,7 @@ struct ImplicitSolver {
     DevBuf d_idx, d_info, d_prm, d_eblk, d_row, d_col, d_val, d_diag, d_mass;
     DevBuf d_x, d_v, d_x0, d_v0, d_vi, d_xm1, d_vm1, d_f, d_b, d_u, d_w;
     DevBuf d_dx, d_r, d_z, d_p, d_Ap, d_dinv, d_dots, d_ctl;
+    DevBuf d_val2, d_p2, d_wide;  // the CG's double-float matrix and direction, and the range flag
     HostBuf h_dots, h_ctl;
     cudaGraphExec_t cg_graph{nullptr};
     ImplicitTables T{};
@@ -630,12 +921,16 @@ struct ImplicitSolver {
         for (DevBuf *b : {&d_x, &d_v, &d_x0, &d_v0, &d_vi, &d_xm1, &d_vm1, &d_f, &d_b, &d_u, &d_w, &d_dx, &d_r, &d_z,
                           &d_p, &d_Ap, &d_dinv})
             SPGX_TRY_STATUS(b->alloc(vb));
+        SPGX_TRY_STATUS(d_val2.alloc(size_t(std::max(1, nnzb)) * 9 * sizeof(float2)));
+        SPGX_TRY_STATUS(d_p2.alloc(size_t(std::max(1, nv)) * 3 * sizeof(float2)));
+        SPGX_TRY_STATUS(d_wide.alloc(sizeof(int)));
         SPGX_TRY_STATUS(d_dots.alloc(size_t(8) * sizeof(double)));
         SPGX_TRY_STATUS(h_dots.alloc(size_t(8) * sizeof(double)));
         SPGX_TRY_STATUS(d_ctl.alloc(sizeof(CgControl)));
         SPGX_TRY_STATUS(h_ctl.alloc(sizeof(CgControl)));
         T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
-                           d_col.as<int>(), d_val.as<double>(), d_diag.as<int>()};
+                           d_col.as<int>(), d_val.as<double>(), d_diag.as<int>(), d_val2.as<float2>(),
+                           d_wide.as<int>()};
         std::vector<double> x(3 * size_t(std::max(1, nv)), 0.0), v(x.size(), 0.0);
         for (int i = 0; i < nv; ++i) {
             const int k = L.ext2int[i];
@@ -692,11 +987,12 @@ struct ImplicitSolver {
         for (int it = 0; it < kCgChunk; ++it) {
             double *prev = it % 2 == 0 ? A : B, *cur = it % 2 == 0 ? B : A;
             cudaMemsetAsync(prev, 0, sizeof(double), stream);
-            launch_spmv(T, vec(d_p), vec(d_Ap), nv, prev, ctl, stream);
+            launch_spmv(T, vec(d_p), vec(d_Ap), nv, prev, ctl, stream, d_p2.as<float2>());
             cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream);
-            implicit_cg_update_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
+            implicit_cg_update_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
                                                                      vec(d_Ap), vec(d_dinv), n, prev, cur, ctl);
-            implicit_cg_direction_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_p), vec(d_z), n, prev, cur, ctl);
+            implicit_cg_direction_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_p), d_p2.as<float2>(), T.wide,
+                                                                        vec(d_z), n, prev, cur, ctl);
         }
         const cudaError_t ce = cudaStreamEndCapture(stream, &g);
         if (ce != cudaSuccess) {
@@ -719,10 +1015,12 @@ struct ImplicitSolver {
     {
         const int nv = L.nv, n = n3();
         implicit_lhs_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_mass), nv, alpha, beta, vec(d_dinv));
+        SPGX_CUDA(cudaMemsetAsync(T.wide, 0, sizeof(int), stream));
+        implicit_split_kernel<<<kSplitBlocks, 256, 0, stream>>>(T, size_t(nnzb) * 9, nv);
         double *dots = d_dots.as<double>();  // two sets of {pAp, rr, rz}: [0..2] and [3..5]
         SPGX_CUDA(cudaMemsetAsync(dots, 0, 6 * sizeof(double), stream));
-        implicit_cg_init_kernel<<<grid_of(n), 256, 0, stream>>>(vec(d_b), vec(d_dinv), vec(d_dx), vec(d_r), vec(d_z),
-                                                                vec(d_p), n, dots);
+        implicit_cg_init_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_b), vec(d_dinv), vec(d_dx), vec(d_r), vec(d_z),
+                                                                vec(d_p), d_p2.as<float2>(), T.wide, n, dots);
         implicit_cg_control_kernel<<<1, 1, 0, stream>>>(d_ctl.as<CgControl>(), dots, P.cg_threshold,
                                                         P.cg_max_iterations);
         SPGX_CUDA(cudaGetLastError());
