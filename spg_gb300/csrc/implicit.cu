@@ -58,8 +58,10 @@ struct ImplicitTables {
     const int *col;      // BSR block columns
     double *val;         // BSR values, 9 per block (row-major)
     const int *diag;     // per vertex: position of its diagonal block
-    float2 *val2;        // the CG's system matrix in double-float form (split_df), 9 per block
+    float2 *val2;        // the CG's system matrix in double-float form (split_df), entry-major:
+                         // entry q (row-major in the block) of block k at val2[q * nnzb + k]
     int *wide;           // set when the CG's matrix or direction leaves the double-float range
+    int nnzb;            // number of blocks
 };
 
 // Double-float form of an FP64 value: a = hi + lo with hi = fl32(a) and lo = fl32(a - hi),
@@ -395,15 +397,19 @@ __global__ void implicit_lhs_kernel(ImplicitTables T, const double *mass, int nv
     dinv[3 * i + 2] = b[8] != 0.0 ? 1.0 / b[8] : 1.0;
 }
 
-// val2 = split_df(val) over all 9 nnzb values. A nonzero diagonal below 2^-60 in magnitude
-// (a row whose scale nears FP32's underflow) also selects the FP64 SpMV.
+// val2 = split_df(val) over all 9 nnzb values, transposed to the entry-major layout (the
+// SpMV's lanes then read consecutive blocks with coalesced 8-byte loads). A nonzero
+// diagonal below 2^-60 in magnitude (a row whose scale nears FP32's underflow) also selects
+// the FP64 SpMV.
 __global__ void implicit_split_kernel(ImplicitTables T, size_t n_values, int nv)
 {
     bool bad = false;
-    for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n_values; k += size_t(gridDim.x) * blockDim.x) {
-        bool o;
-        T.val2[k] = split_df(T.val[k], o);
-        bad |= o;
+    const size_t nb = size_t(T.nnzb);
+    for (size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x; o < n_values; o += size_t(gridDim.x) * blockDim.x) {
+        const size_t q = o / nb, k = o - q * nb;
+        bool out;
+        T.val2[o] = split_df(T.val[k * 9 + q], out);
+        bad |= out;
     }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
         const double *d = T.val + size_t(T.diag[i]) * 9;
@@ -439,7 +445,19 @@ __device__ __forceinline__ void block_reduce_add2(double a, double b, double *oa
     }
 }
 
-__device__ __forceinline__ void block_reduce_add(double v, double *out) { block_reduce_add2(v, 0.0, out, nullptr); }
+__device__ __forceinline__ void block_reduce_add(double v, double *out)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ double part1[32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) part1[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (blockDim.x + 31) / 32; ++k) s += part1[k];
+        atomicAdd(out, s);
+    }
+}
 
 // Device-side control of one CG solve: the iteration loop runs as captured graphs of several
 // iterations with no host round trip per iteration; once done is set every later kernel of
@@ -507,19 +525,21 @@ __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict_
         float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
         if (i < nv) {
             const int k1 = __ldg(T.row_ptr + i + 1);
+#pragma unroll 2
+            const size_t nb = size_t(T.nnzb);
             for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
-                const float2 *bl = T.val2 + size_t(k) * 9;
+                const float2 *bl = T.val2 + k;
                 const float2 *x = p2 + 3 * size_t(__ldg(T.col + k));
                 const float2 x0 = x[0], x1 = x[1], x2 = x[2];
-                df_fma(h0, l0, bl[0], x0);
-                df_fma(h0, l0, bl[1], x1);
-                df_fma(h0, l0, bl[2], x2);
-                df_fma(h1, l1, bl[3], x0);
-                df_fma(h1, l1, bl[4], x1);
-                df_fma(h1, l1, bl[5], x2);
-                df_fma(h2, l2, bl[6], x0);
-                df_fma(h2, l2, bl[7], x1);
-                df_fma(h2, l2, bl[8], x2);
+                df_fma(h0, l0, __ldg(bl), x0);
+                df_fma(h0, l0, __ldg(bl + nb), x1);
+                df_fma(h0, l0, __ldg(bl + 2 * nb), x2);
+                df_fma(h1, l1, __ldg(bl + 3 * nb), x0);
+                df_fma(h1, l1, __ldg(bl + 4 * nb), x1);
+                df_fma(h1, l1, __ldg(bl + 5 * nb), x2);
+                df_fma(h2, l2, __ldg(bl + 6 * nb), x0);
+                df_fma(h2, l2, __ldg(bl + 7 * nb), x1);
+                df_fma(h2, l2, __ldg(bl + 8 * nb), x2);
             }
         }
 #pragma unroll
@@ -528,11 +548,35 @@ __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict_
             df_add(h1, l1, __shfl_xor_sync(0xffffffffu, h1, o), __shfl_xor_sync(0xffffffffu, l1, o));
             df_add(h2, l2, __shfl_xor_sync(0xffffffffu, h2, o), __shfl_xor_sync(0xffffffffu, l2, o));
         }
-        if (lane == 0) {
-            y0 = double(h0) + double(l0);
-            y1 = double(h1) + double(l1);
-            y2 = double(h2) + double(l2);
+        // p . Ap in double-float as well: lane 0 of each row forms its row's product, the
+        // warp reduces in double-float, and only the warp sums meet in FP64.
+        float ph = 0.f, pl = 0.f;
+        if (i < nv && lane == 0) {
+            Ap[3 * i] = double(h0) + double(l0);
+            Ap[3 * i + 1] = double(h1) + double(l1);
+            Ap[3 * i + 2] = double(h2) + double(l2);
+            if (dots) {
+                const float2 *pi = p2 + 3 * size_t(i);
+                df_fma(ph, pl, pi[0], make_float2(h0, l0));
+                df_fma(ph, pl, pi[1], make_float2(h1, l1));
+                df_fma(ph, pl, pi[2], make_float2(h2, l2));
+            }
         }
+        if (dots) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                df_add(ph, pl, __shfl_xor_sync(0xffffffffu, ph, o), __shfl_xor_sync(0xffffffffu, pl, o));
+            __shared__ double part_df[32];
+            const int w = threadIdx.x >> 5;
+            if ((threadIdx.x & 31) == 0) part_df[w] = double(ph) + double(pl);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double sum = 0.0;
+                for (int k = 0; k < (blockDim.x + 31) / 32; ++k) sum += part_df[k];
+                atomicAdd(dots, sum);
+            }
+        }
+        return;
     } else {
         if (i < nv) {
             const int k1 = __ldg(T.row_ptr + i + 1);
@@ -582,6 +626,7 @@ __global__ void implicit_cg_init_kernel(const double *b, const double *dinv, dou
 {
     double rr = 0.0, rz = 0.0;
     bool bad = false;
+#pragma unroll 4
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double ri = b[i], zi = ri * dinv[i];
         x[i] = 0.0;
@@ -621,6 +666,7 @@ __global__ void implicit_cg_update_kernel(double *x, double *r, double *z, const
     __syncthreads();
     const double alpha = s_alpha;
     double rr = 0.0, rz = 0.0;
+#pragma unroll 4
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
         const double ri = r[i] - alpha * Ap[i];
@@ -653,6 +699,7 @@ __global__ void implicit_cg_direction_kernel(double *p, float2 *p2, int *wide, c
     __syncthreads();
     const double beta = s_beta;
     bool bad = false;
+#pragma unroll 4
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double pi = z[i] + beta * p[i];
         p[i] = pi;
@@ -778,8 +825,8 @@ __global__ void symplectic_kernel(double *v, const double *f, const double *mass
 
 static int grid_of(int n, int t = 256) { return (n + t - 1) / t; }
 // The CG's vector kernels loop over several entries per thread, so their FP64 block
-// reductions (a shuffle tree per thread) are paid once per few entries: 8 blocks of 256 per SM.
-static int cg_grid(int n) { return std::max(1, std::min(grid_of(n), 152 * 8)); }
+// reductions (a shuffle tree per thread) are paid once per few entries: 4 blocks of 256 per SM.
+static int cg_grid(int n) { return std::max(1, std::min(grid_of(n), 152 * 4)); }
 
 struct ImplicitSolver {
     SceneLayout L;
@@ -930,7 +977,7 @@ struct ImplicitSolver {
         SPGX_TRY_STATUS(h_ctl.alloc(sizeof(CgControl)));
         T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
                            d_col.as<int>(), d_val.as<double>(), d_diag.as<int>(), d_val2.as<float2>(),
-                           d_wide.as<int>()};
+                           d_wide.as<int>(), nnzb};
         std::vector<double> x(3 * size_t(std::max(1, nv)), 0.0), v(x.size(), 0.0);
         for (int i = 0; i < nv; ++i) {
             const int k = L.ext2int[i];
