@@ -377,7 +377,10 @@ int32_t spgx_num_constraints(int32_t type);
  * force, stiffness matrix and conjugate-gradient solve (implicitEulerBase.cpp:102-240):
  * f = M g - grad E(x), K = -hess E(x) (full element Hessians, no definiteness projection),
  * linear systems by CG with the diagonal preconditioner (relative tolerance cg_threshold,
- * cg_max_iterations, zero start). State, assembly and solve are FP64. Per substep of h:
+ * cg_max_iterations, zero start). State, assembly and the CG's vectors and dot products are
+ * FP64; the CG's matrix-vector products run in double-float (FP32 pairs, 48-bit significands)
+ * unless a matrix value or direction entry exceeds 2^60 in magnitude (or a nonzero diagonal
+ * is below 2^-60), in which case that solve's products run in FP64. Per substep of h:
  *   NEWTON_DX       implicitEulerNewtonDx.cpp:31-55     x += v h; (M/h^2 - K) dx = f; x += dx; v = (x - x0)/h
  *   NEWTON_DV       implicitEulerNewtonDv.cpp:31-60     x += v h; (M - h^2 K) dv = h f; v = v0 + dv; x = x0 + v h
  *   NEWTON_ROBUST   implicitEulerNewtonRobust.cpp:33-126 Newton on (M - h^2 K) dv = h f - M (v_i - v0) with a
@@ -395,7 +398,8 @@ int32_t spgx_num_constraints(int32_t type);
  * substeps; converged = every solve reached cg_threshold (robust methods: every substep
  * succeeded); residual_final = the last solve's relative residual |r| / |b| (robust methods:
  * the last Newton residual norm, residual_initial the first); fallback_solves = Newton
- * iterations and skipped_solves = failed substeps (robust methods). */
+ * iterations and skipped_solves = failed substeps (robust methods); warm_accepted = solves
+ * whose products ran in FP64. */
 typedef enum spgx_implicit_method {
     SPGX_IMPLICIT_NEWTON_DX = 0,          /* spg::solver::ImplicitEulerNewtonDx */
     SPGX_IMPLICIT_NEWTON_DV = 1,          /* spg::solver::ImplicitEulerNewtonDv */

@@ -838,7 +838,7 @@ struct ImplicitSolver {
     DevBuf d_x, d_v, d_x0, d_v0, d_vi, d_xm1, d_vm1, d_f, d_b, d_u, d_w;
     DevBuf d_dx, d_r, d_z, d_p, d_Ap, d_dinv, d_dots, d_ctl;
     DevBuf d_val2, d_p2, d_wide;  // the CG's double-float matrix and direction, and the range flag
-    HostBuf h_dots, h_ctl;
+    HostBuf h_dots, h_ctl, h_wide;
     cudaGraphExec_t cg_graph{nullptr};
     ImplicitTables T{};
     int n_elem{0}, nnzb{0};
@@ -975,6 +975,7 @@ struct ImplicitSolver {
         SPGX_TRY_STATUS(h_dots.alloc(size_t(8) * sizeof(double)));
         SPGX_TRY_STATUS(d_ctl.alloc(sizeof(CgControl)));
         SPGX_TRY_STATUS(h_ctl.alloc(sizeof(CgControl)));
+        SPGX_TRY_STATUS(h_wide.alloc(sizeof(int)));
         T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
                            d_col.as<int>(), d_val.as<double>(), d_diag.as<int>(), d_val2.as<float2>(),
                            d_wide.as<int>(), nnzb};
@@ -1085,13 +1086,18 @@ struct ImplicitSolver {
             set_error("internal: the CG control did not finish");
             return SPGX_ERR_CUDA;
         }
+        SPGX_CUDA(cudaMemcpyAsync(h_wide.as<void>(), T.wide, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        fp64_products = *h_wide.as<int>() != 0;
         iterations = hc->its;
         rel_residual = hc->rr0 > 0.0 ? std::sqrt(hc->rr / hc->rr0) : 0.0;
         return SPGX_OK;
     }
 
+    bool fp64_products{false};  // the last solve's products ran in FP64 (out of double-float range)
+
     struct Tally {
-        int cg_iterations = 0, newton_iterations = 0, failed = 0;
+        int cg_iterations = 0, newton_iterations = 0, failed = 0, fp64_solves = 0;
         bool converged = true;
         double first_residual = -1.0, last_residual = 0.0;
     };
@@ -1102,6 +1108,7 @@ struct ImplicitSolver {
         double rel = 0.0;
         SPGX_TRY_STATUS(cg(alpha, beta, its, rel));
         t.cg_iterations += its;
+        t.fp64_solves += fp64_products ? 1 : 0;
         t.last_residual = rel;
         if (rel > P.cg_threshold) t.converged = false;
         return SPGX_OK;
@@ -1342,6 +1349,7 @@ struct ImplicitSolver {
         st.residual_initial = t.first_residual < 0 ? 0.0 : t.first_residual;
         st.residual_final = t.last_residual;
         st.device_ms = ms;
+        st.warm_accepted = t.fp64_solves;
         if (stats) *stats = st;
         return SPGX_OK;
     }

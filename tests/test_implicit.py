@@ -100,6 +100,32 @@ def test_bending_dominated_cloth_matches_oracle():
     assert err <= 1e-3 * moved
 
 
+@pytest.mark.gpu
+def test_wide_system_runs_fp64_products():
+    """Masses and stiffnesses of the truss scaled by 1e20: the system matrix exceeds the
+    double-float range (2^60), so every CG solve's products run in FP64 (reported in
+    warm_accepted). The motion is the unscaled truss's, and matches the oracle's."""
+    N = pytest.importorskip("spg_gb300.native")
+    S = 1e20
+    base = scenes.truss_variant()
+    wide = scenes.truss_variant(k_cont=2e3 * S, k_sq=5e2 * S)
+    wide.mass = wide.mass * S
+    for e in wide.energies:
+        if e.type == O.ANCHOR:
+            e.params[:, 3] *= S
+    g_wide = N.ImplicitSolver([wide], dt=1 / 60, substeps=1, gravity=scenes.GRAVITY)
+    g_base = N.ImplicitSolver([base], dt=1 / 60, substeps=1, gravity=scenes.GRAVITY)
+    ref = IR.ImplicitEuler(wide, 1 / 60, 1, scenes.GRAVITY)
+    for _ in range(5):
+        assert g_wide.step().warm_accepted == 1
+        assert g_base.step().warm_accepted == 0
+        ref.step()
+    xw, xb, xr = g_wide.state(0)[0], g_base.state(0)[0], ref.state()[0]
+    moved = float(np.abs(xr - wide.x).max())
+    assert np.abs(xw - xr).max() <= 1e-3 * moved
+    assert np.abs(xw - xb).max() <= 1e-3 * moved
+
+
 # ---------------------------------------------------------------------------------------
 # The other global solvers (NewtonDv, NewtonRobust, BaraffWitkin, BDF2, StaticNewton,
 # QuasiStaticNewton, QuasiStaticNewtonRobust, SimplecticEuler), each on scenes where the
