@@ -257,10 +257,9 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         group_reduce<G>(acc);
         if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tg, invdt2, fb2);
         __syncthreads();  // every position of the tile is written, the staging consumed, s_next set
-        if (threadIdx.x == 0) {
-            __threadfence();
-            st_release_gpu(F.epoch + tile, epoch_base + k + 1);
-        }
+        // The release is cumulative: the CTA's position writes, ordered before it by the barrier,
+        // are visible to any CTA that acquires this epoch.
+        if (threadIdx.x == 0) st_release_gpu(F.epoch + tile, epoch_base + k + 1);
         task = s_next;
         if (task < total) fetch_static(task, h0, h1, hv, roff, tg);
     }
