@@ -17,6 +17,9 @@ struct alignas(16) I4 {
 struct alignas(16) F4 {
     float x, y, z, w;
 };
+struct alignas(8) I2 {
+    int32_t x, y;
+};
 struct alignas(8) F2 {
     float x, y;
 };

@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
 // co-resident CTAs (cooperative launch), so the waits always end; each is still bounded, and
 // a wait that gives up sets the abort flag and status bit 1 so that every CTA leaves.
 constexpr int kFlowMaxPolls = 1 << 21;  // with 128 ns sleeps and an L2 round trip: about a second per wait
+constexpr int kFlowPollMax = 64;       // neighbour-list entries prefetched per task (the rest are read directly)
 
 template <int G>
 __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V, const DevState S,
@@ -163,20 +164,44 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     float4 *sb = dyn;
     float4 *sd = dyn + max_local;
     int4 *srec = reinterpret_cast<int4 *>(dyn + 2 * max_local);
+    // The next task's tile header, neighbour-list range and packed neighbour list, copied while
+    // the current task stages and computes, so that no global round trip is spent on them
+    // between two tasks.
+    __shared__ int4 s_hdr[2];
+    __shared__ int2 s_fh;
+    __shared__ int s_poll[kFlowPollMax];
     __shared__ int s_next, s_fail;
     const int total = iterations * n_tiles;
     const int lv = threadIdx.x / G;
     const int lane = threadIdx.x & (G - 1);
     int *sidx = reinterpret_cast<int *>(srec + V.max_records);
 
+    // Thread 0: the header and neighbour-list range of task t, async (waited with the staging).
+    auto prefetch_header = [&](int t) {
+        if (threadIdx.x == 0 && t < total) {
+            const int tile = t % n_tiles;
+            cp_async16(s_hdr, V.hdr + 2 * tile);
+            cp_async16(s_hdr + 1, V.hdr + 2 * tile + 1);
+            cp_async8(&s_fh, F.fhdr + tile);
+        }
+    };
+    // Warp 0: the first kFlowPollMax entries of task t's neighbour list, async, as one group
+    // (each lane later reads only the entries it copied). Needs s_fh.
+    auto prefetch_poll = [&](int t) {
+        if (threadIdx.x < 32 && t < total) {
+            const int2 fh = s_fh;
+            const int n = min(fh.y, kFlowPollMax);
+            for (int j = threadIdx.x; j < n; j += 32) cp_async4(s_poll + j, F.nbrp + fh.x + j);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+    };
     // Static data of a task, fetched while the previous task finishes or its dependencies are
-    // polled: its header, its record block and the indices of its local vertices (both into
-    // shared memory, async), and the header, record offset and inertial target of the thread's
-    // vertex. The target y is fixed for the whole step.
-    auto fetch_static = [&](int task, int4 &h0, int4 &h1, int4 &hv, int &roff, float4 &tg) {
-        const int tile = task % n_tiles;
-        h0 = __ldg(V.hdr + 2 * tile);
-        h1 = __ldg(V.hdr + 2 * tile + 1);
+    // polled: its record block and the indices of its local vertices (both into shared memory,
+    // async), and the header, record offset and inertial target of the thread's vertex. The
+    // target y is fixed for the whole step. The tile header comes from the prefetch.
+    auto fetch_static = [&](int4 &h0, int4 &h1, int4 &hv, int &roff, float4 &tg) {
+        h0 = s_hdr[0];
+        h1 = s_hdr[1];
         const int nvt = h0.y, nl = h0.y + h0.w;
         for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
         for (int i = threadIdx.x; i < nl; i += blockDim.x) {
@@ -199,21 +224,30 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     if (threadIdx.x == 0) s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
     __syncthreads();
     int task = s_next;
+    prefetch_header(task);
+    cp_async_wait_all();
+    __syncthreads();
+    prefetch_poll(task);
     int4 h0, h1, hv;
     int roff;
     float4 tg;
-    if (task < total) fetch_static(task, h0, h1, hv, roff, tg);
+    if (task < total) fetch_static(h0, h1, hv, roff, tg);
     while (task < total) {
         const int k = task / n_tiles;
         const int tile = task - k * n_tiles;
-        // Wait for the tiles this sweep reads (warp 0 polls, one neighbour per lane).
+        // Wait for the tiles this sweep reads (warp 0 polls, one neighbour per lane). Thread 0
+        // also takes the next ticket, so that the next task's header can be prefetched while
+        // this one runs; a task still waits only on tasks with smaller tickets.
         if (threadIdx.x < 32) {
-            const int c = __ldg(F.tile_color + tile);
-            const int b = __ldg(F.nbr_off + tile), e = __ldg(F.nbr_off + tile + 1);
+            int ticket = total;
+            if (threadIdx.x == 0) ticket = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this lane's neighbour entries
+            const int2 fh = s_fh;
             bool ok = true;
-            for (int j = b + threadIdx.x; j < e && ok; j += 32) {
-                const int u = __ldg(F.nbr + j);
-                const int need = epoch_base + k + (__ldg(F.tile_color + u) < c ? 1 : 0);
+            for (int j = threadIdx.x; j < fh.y && ok; j += 32) {
+                const int pk = j < kFlowPollMax ? s_poll[j] : __ldg(F.nbrp + fh.x + j);
+                const int u = pk & 0x7fffffff;
+                const int need = epoch_base + k + (pk < 0 ? 1 : 0);
                 int polls = 0;
                 while (ld_acquire_gpu(F.epoch + u) < need) {
                     if (++polls > kFlowMaxPolls || ld_relaxed_gpu(F.ticket + 1)) {
@@ -224,10 +258,13 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
                 }
             }
             ok = __all_sync(0xffffffffu, ok);
-            if (threadIdx.x == 0) s_fail = !ok;
+            if (threadIdx.x == 0) {
+                s_fail = !ok;
+                s_next = ticket;
+            }
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // this thread's index and record copies
-        __syncthreads();  // every thread's index and record copies, and the poll result
+        __syncthreads();  // every thread's index and record copies, the poll result and s_next
         if (s_fail) {
             if (threadIdx.x == 0) {
                 atomicExch(F.ticket + 1, 1);
@@ -235,6 +272,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             }
             break;
         }
+        prefetch_header(s_next);
         // Stage the current positions of the local vertices.
         const int nl = h0.y + h0.w;
         for (int i = threadIdx.x; i < nl; i += blockDim.x) {
@@ -243,9 +281,9 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
             cp_async16(sd + i, S.pos + 2 * g + 1);
         }
         const bool active = lv < h0.y;
-        if (threadIdx.x == 0) s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
         cp_async_wait_all();
-        __syncthreads();
+        __syncthreads();  // the staging and the next task's header
+        prefetch_poll(s_next);
         TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
         if (active) {
             cx.bs = v3(sb[lv]);
@@ -256,12 +294,12 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
         group_reduce<G>(acc);
         if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tg, invdt2, fb2);
-        __syncthreads();  // every position of the tile is written, the staging consumed, s_next set
+        __syncthreads();  // every position of the tile is written and the staging consumed
         // The release is cumulative: the CTA's position writes, ordered before it by the barrier,
         // are visible to any CTA that acquires this epoch.
         if (threadIdx.x == 0) st_release_gpu(F.epoch + tile, epoch_base + k + 1);
         task = s_next;
-        if (task < total) fetch_static(task, h0, h1, hv, roff, tg);
+        if (task < total) fetch_static(h0, h1, hv, roff, tg);
     }
 }
 
@@ -652,14 +690,19 @@ spgx_status VbdSolver::setup_tiles(int tv)
     // block just under the 48 KB default.
     int optin = 0;
     SPGX_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-    const int cap = optin - 256;
+    const int cap = optin - 512;  // room for the kernels' static shared memory (304 bytes at most)
     if (tile_smem > size_t(cap)) {
         set_error("a tile needs more shared memory than the device offers; lower tile_vertices");
         return SPGX_ERR_INVALID_ARG;
     }
     {
-        auto raise = [cap](const void *fn) -> cudaError_t {
-            return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+        // Each kernel may take the opt-in limit less its own static shared memory.
+        auto raise = [optin](const void *fn) -> cudaError_t {
+            cudaFuncAttributes a{};
+            const cudaError_t e = cudaFuncGetAttributes(&a, fn);
+            if (e != cudaSuccess) return e;
+            return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        optin - static_cast<int>(a.sharedSizeBytes));
         };
         SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<1>)));
         SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<2>)));
@@ -689,7 +732,8 @@ spgx_status VbdSolver::setup_flow()
             const I4 h = TL.hdr[2 * t];
             for (int i = 0; i < h.y; ++i) tile_of[h.x + i] = t;
         }
-    std::vector<int32_t> off(n_tiles + 1, 0), nbr;
+    std::vector<int32_t> nbr;
+    std::vector<I2> fhdr(std::max(1, n_tiles), I2{0, 0});
     std::vector<int32_t> tmp;
     for (int t = 0; t < n_tiles; ++t) {
         const I4 h = TL.hdr[2 * t];
@@ -701,16 +745,15 @@ spgx_status VbdSolver::setup_flow()
             set_error("internal: a halo vertex belongs to no tile");
             return SPGX_ERR_INVALID_ARG;
         }
-        nbr.insert(nbr.end(), tmp.begin(), tmp.end());
-        off[t + 1] = static_cast<int32_t>(nbr.size());
+        fhdr[t] = I2{static_cast<int32_t>(nbr.size()), static_cast<int32_t>(tmp.size())};
+        for (int u : tmp) nbr.push_back(color[u] < color[t] ? static_cast<int32_t>(uint32_t(u) | 0x80000000u) : u);
     }
     if (nbr.empty()) nbr.push_back(0);
-    SPGX_TRY_STATUS(fl_nbr_off.upload(off));
-    SPGX_TRY_STATUS(fl_nbr.upload(nbr));
-    SPGX_TRY_STATUS(fl_color.upload(color));
+    SPGX_TRY_STATUS(fl_fhdr.upload(fhdr));
+    SPGX_TRY_STATUS(fl_nbrp.upload(nbr));
     SPGX_TRY_STATUS(fl_epoch.alloc(size_t(std::max(1, n_tiles)) * sizeof(int)));
     SPGX_TRY_STATUS(fl_ticket.alloc(2 * sizeof(int)));
-    FV = FlowView{fl_nbr_off.as<int>(), fl_nbr.as<int>(), fl_color.as<int>(), fl_epoch.as<int>(), fl_ticket.as<int>()};
+    FV = FlowView{fl_fhdr.as<int2>(), fl_nbrp.as<int>(), fl_epoch.as<int>(), fl_ticket.as<int>()};
     SPGX_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
     const int T = TL.tile_vertices;
     const void *fns[4] = {reinterpret_cast<const void *>(vbd_flow_kernel<1>),

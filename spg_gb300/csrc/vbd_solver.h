@@ -45,7 +45,7 @@ struct VbdSolver {
     DevBuf tb_hdr, tb_halo, tb_records, tb_vrec;
     TileView TV{};
     size_t tile_smem{0};
-    DevBuf fl_nbr_off, fl_nbr, fl_color, fl_epoch, fl_ticket;
+    DevBuf fl_fhdr, fl_nbrp, fl_epoch, fl_ticket;
     FlowView FV{};
     int flow_blocks_per_sm[4]{};  // per lanes variant 1, 2, 4, 8
     int num_sms{0};

@@ -30,11 +30,11 @@ struct TileView {
 
 // Tables of the dataflow kernel (vbd_flow_kernel).
 struct FlowView {
-    const int *nbr_off;     // per tile: range in nbr
-    const int *nbr;         // neighbour tiles (self included)
-    const int *tile_color;  // colour of each tile
-    int *epoch;             // per tile: sweeps completed (monotonic over launches)
-    int *ticket;            // [0] next task, [1] abort flag (both zeroed before a launch)
+    const int2 *fhdr;  // per tile: {first entry in nbrp, number of entries}
+    const int *nbrp;   // neighbour tiles (self included): tile id, with bit 31 set when that
+                       // tile's colour is lower than the owner's (its current sweep is awaited)
+    int *epoch;        // per tile: sweeps completed (monotonic over launches)
+    int *ticket;       // [0] next task, [1] abort flag (both zeroed before a launch)
 };
 
 // Positions (base + delta) of the local vertices and the record block; the dataflow kernel
@@ -48,6 +48,12 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
