@@ -148,7 +148,10 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
 // colours prescribes. Higher-colour neighbours cannot overwrite T's inputs early, because
 // they in turn wait for T. Each task waits only on tasks with smaller tickets, all held by
 // co-resident CTAs (cooperative launch), so the waits always end; each is still bounded, and
-// a wait that gives up sets the abort flag and status bit 1 so that every CTA leaves.
+// a wait that gives up sets the abort flag and status bit 1 so that every CTA leaves. A CTA
+// takes its next ticket while it polls for the current one: the smallest unfinished ticket is
+// then always running (a CTA holding it unstarted would be running a smaller unfinished one),
+// so progress is kept.
 constexpr int kFlowMaxPolls = 1 << 21;  // with 128 ns sleeps and an L2 round trip: about a second per wait
 constexpr int kFlowPollMax = 64;       // neighbour-list entries prefetched per task (the rest are read directly)
 
