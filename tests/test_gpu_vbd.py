@@ -164,7 +164,7 @@ def test_colors_and_adjacency_through_handle():
     assert np.array_equal(c1, c2) and np.array_equal(e1, e2)
 
 
-@pytest.mark.parametrize("lanes,tile", [(1, 64), (2, 64), (4, 64), (4, 32), (2, 32)])
+@pytest.mark.parametrize("lanes,tile", [(1, 64), (2, 64), (4, 64), (4, 32), (2, 32), (4, 16), (8, 16)])
 def test_dataflow_kernel_equals_colour_launches(lanes, tile):
     """The dataflow kernel runs the same Gauss-Seidel order as one launch per colour, so with
     the same lanes per vertex (same per-vertex summation order) it gives the same positions
