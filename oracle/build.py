@@ -14,7 +14,17 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root() -> str:
+    """The reference checkout: $SPG_REFERENCE_ROOT, else a directory named `reference` beside
+    this repository's root. When it is absent the reference's colouring is not built (the GPU
+    hosts have no checkout; the tests that need it skip)."""
+    env = os.environ.get("SPG_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
 
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp"]
 
@@ -42,8 +52,9 @@ def oracle_command() -> tuple[list[str], str, list[str]]:
 
 
 def ref_command() -> tuple[list[str], str, list[str]] | None:
-    src = os.path.join(REFERENCE_ROOT, "spg", "source", "utils", "graphColoring.cpp")
-    inc = os.path.join(REFERENCE_ROOT, "spg", "include")
+    root = reference_root()
+    src = os.path.join(root, "spg", "source", "utils", "graphColoring.cpp")
+    inc = os.path.join(root, "spg", "include")
     if not os.path.exists(src):
         return None
     shim = os.path.join(HERE, "ref_coloring_shim.cpp")

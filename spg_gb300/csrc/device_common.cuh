@@ -95,6 +95,19 @@ __device__ __forceinline__ V3f rel_pos(const float4 *__restrict__ pos, int j, V3
     return mk((b.x - bs.x) + (d.x - ds.x), (b.y - bs.y) + (d.y - ds.y), (b.z - bs.z) + (d.z - ds.z));
 }
 
+// The same as hi + lo, where lo is the rounding remainder of adding the base and delta
+// differences (an error-free sum), for the spring stretch.
+__device__ __forceinline__ V3f rel_pos2(const float4 *__restrict__ pos, int j, V3f bs, V3f ds, V3f &lo)
+{
+    const float4 b = __ldg(pos + 2 * j);
+    const float4 d = __ldg(pos + 2 * j + 1);
+    V3f hi;
+    two_sum(b.x - bs.x, d.x - ds.x, hi.x, lo.x);
+    two_sum(b.y - bs.y, d.y - ds.y, hi.y, lo.y);
+    two_sum(b.z - bs.z, d.z - ds.z, hi.z, lo.z);
+    return hi;
+}
+
 __device__ __forceinline__ int warp_max(int v) { return __reduce_max_sync(0xffffffffu, v); }
 
 // Waits until the previous kernel on the stream has completed and its writes are visible
@@ -159,8 +172,9 @@ __device__ __forceinline__ void accumulate_incidences(const DevTables &T, const 
                 const int ent = __ldg(adj + off + i);
                 const int4 s = __ldg(T.springs + (ent >> 2));
                 const int o = (ent & 3) ? s.x : s.y;
-                const V3f po = rel_pos(pos, o, bs, ds);
-                spring_block(zero, po, __int_as_float(s.z), __int_as_float(s.w), acc);
+                V3f lo;
+                const V3f po = rel_pos2(pos, o, bs, ds, lo);
+                spring_block(zero, po, mk(-lo.x, -lo.y, -lo.z), __int_as_float(s.z), __int_as_float(s.w), acc);
             }
         }
         off += n;
@@ -294,6 +308,19 @@ __device__ __forceinline__ void group_reduce(Block<float> &acc)
 #pragma unroll
         for (int k = 0; k < 6; ++k) acc.h[k] += __shfl_xor_sync(0xffffffffu, acc.h[k], o);
     }
+}
+
+// Three lanes per vertex (lanes 3g, 3g + 1, 3g + 2 of a warp): the first lane of each group
+// ends with the total (the others, and the two idle lanes 30 and 31, with partial sums).
+template <>
+__device__ __forceinline__ void group_reduce<3>(Block<float> &acc)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        acc.f[k] += __shfl_down_sync(0xffffffffu, acc.f[k], 1) + __shfl_down_sync(0xffffffffu, acc.f[k], 2);
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        acc.h[k] += __shfl_down_sync(0xffffffffu, acc.h[k], 1) + __shfl_down_sync(0xffffffffu, acc.h[k], 2);
 }
 
 }  // namespace spgx

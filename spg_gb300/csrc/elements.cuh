@@ -181,19 +181,76 @@ SPGX_HD void anchor_block(Vec3<T> x, Vec3<T> a, T k, Block<T> &b)
     add_diag(b, k);
 }
 
+SPGX_HD float fmadd(float a, float b, float c) { return fmaf(a, b, c); }
+SPGX_HD double fmadd(double a, double b, double c) { return fma(a, b, c); }
+// A product and a sum that the device compiler never fuses into an FMA with a neighbouring
+// operation (error-free transformations need each one rounded on its own; the host build
+// disables contraction altogether).
+#if defined(__CUDA_ARCH__)
+SPGX_HD float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+SPGX_HD double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+SPGX_HD float add_rn(float a, float b) { return __fadd_rn(a, b); }
+SPGX_HD double add_rn(double a, double b) { return __dadd_rn(a, b); }
+#else
+SPGX_HD float mul_rn(float a, float b) { return a * b; }
+SPGX_HD double mul_rn(double a, double b) { return a * b; }
+SPGX_HD float add_rn(float a, float b) { return a + b; }
+SPGX_HD double add_rn(double a, double b) { return a + b; }
+#endif
+
+// Knuth's error-free sum: a + b = s + e exactly, for any ordering of |a| and |b|.
+template <typename T>
+SPGX_HD void two_sum(T a, T b, T &s, T &e)
+{
+    s = add_rn(a, b);
+    const T bb = add_rn(s, -a);
+    e = add_rn(add_rn(a, -add_rn(s, -bb)), add_rn(b, -bb));
+}
+
+// Spring stretch l - L0 for the spring vector s = sh + sl (sl a small remainder of sh's
+// rounding), with l ~ |sh| for the denominator. Near rest l - L0 is a small difference of
+// two nearly equal lengths, and forming it as l - L0 from a rounded l leaves a relative error
+// of about (rounding of l) / strain: 1e-7 / 1e-5 = 1e-2 at a strain of 1e-5. Here
+// |s|^2 - L0^2 is formed without that cancellation: the squares are error-free products
+// (p + e = a * a exactly, e from one FMA), their sum and the subtraction of L0^2 are
+// error-free sums, and only the small remainders are rounded. Then
+// l - L0 = (|s|^2 - L0^2) / (l + L0), where the rounding of l no longer cancels.
+template <typename T>
+SPGX_HD T spring_stretch(Vec3<T> sh, Vec3<T> sl, T L0, T l)
+{
+    const T px = mul_rn(sh.x, sh.x), py = mul_rn(sh.y, sh.y), pz = mul_rn(sh.z, sh.z), q = mul_rn(L0, L0);
+    const T ex = fmadd(sh.x, sh.x, -px), ey = fmadd(sh.y, sh.y, -py);
+    const T ez = fmadd(sh.z, sh.z, -pz), eq = fmadd(L0, L0, -q);
+    T s1, t1, s2, t2, s3, t3;
+    two_sum(px, py, s1, t1);
+    two_sum(s1, pz, s2, t2);
+    two_sum(s2, -q, s3, t3);
+    const T tail = ((ex + ey) + (ez - eq)) + ((t1 + t2) + t3) + T(2) * dot(sh, sl);
+    return (s3 + tail) * recip(l + L0);
+}
+
 // SpringEnergy gradient / Hessian (springEnergy.cpp:101-133) for the vertex xi of a spring
 // whose other end is xo: g = k (l - L0) s / l with s = xi - xo, and
 // H = k [(1 - L0/l)(I - s s^T / l^2) + s s^T / l^2] = k (1 - L0/l) I + k L0 / l^3 s s^T.
+// sl is the remainder of the spring vector's rounding (s = (xi - xo) + sl exactly, or as
+// exactly as the caller knows it); it enters only the stretch l - L0.
 template <typename T>
-SPGX_HD void spring_block(Vec3<T> xi, Vec3<T> xo, T L0, T k, Block<T> &b)
+SPGX_HD void spring_block(Vec3<T> xi, Vec3<T> xo, Vec3<T> sl, T L0, T k, Block<T> &b)
 {
     const Vec3<T> s = xi - xo;
     const T l2 = dot(s, s);
     const T il = rsqrt_of(l2);
     const T l = l2 * il;
-    sub_force(b, s, k * (l - L0) * il);
-    add_diag(b, k * (T(1) - L0 * il));
+    const T c = k * spring_stretch(s, sl, L0, l) * il;  // k (l - L0) / l = k (1 - L0 / l)
+    sub_force(b, s, c);
+    add_diag(b, c);
     add_outer(b, s, k * L0 * il * il * il);
+}
+
+template <typename T>
+SPGX_HD void spring_block(Vec3<T> xi, Vec3<T> xo, T L0, T k, Block<T> &b)
+{
+    spring_block(xi, xo, mk(T(0), T(0), T(0)), L0, k, b);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -3,7 +3,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 #include <vector>
 
 #include "api_internal.h"
@@ -31,7 +30,16 @@ __global__ void eval_blocks_kernel(int type, int n, int S, int P, const float *_
     Block<float> b;
     block_zero(b);
     switch (type) {
-    case SPGX_ENERGY_SPRING: spring_block(zero, r[1 - slot], p[0], p[1], b); break;
+    case SPGX_ENERGY_SPRING: {
+        // s = self - other = -r[other] exactly as s_hi + s_lo (error-free difference).
+        const int o = 1 - slot;
+        V3f sh, sl;
+        two_sum(self.x, -x[3 * o], sh.x, sl.x);
+        two_sum(self.y, -x[3 * o + 1], sh.y, sl.y);
+        two_sum(self.z, -x[3 * o + 2], sh.z, sl.z);
+        spring_block(sh, zero, sl, p[0], p[1], b);
+        break;
+    }
     case SPGX_ENERGY_SPRING_ANCHOR: anchor_block(mk(self.x - p[0], self.y - p[1], self.z - p[2]), zero, p[3], b); break;
     case SPGX_ENERGY_DISCRETE_BENDING:
         if (slot >= 2)
@@ -143,29 +151,20 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-// Device address of the scratch array on the current device, looked up once per device with
-// that device current (the host-side symbol is only a stand-in, never a device address).
+// Device address of the scratch array on the current device (the host-side symbol is only a
+// stand-in, never a device address). The first lookup on a device loads this file's device
+// code there, which places the array. The address is looked up on every call rather than
+// cached: the lookup allocates nothing, and a cached address would go stale if the caller
+// reset the device (the module, and the array with it, is then placed anew).
 static spgx_status noalloc_scratch(NoAllocScratch **out)
 {
-    static std::mutex mutex;
-    static NoAllocScratch *addr[256] = {};
-    int dev = 0;
-    SPGX_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) {
-        set_error("device ordinal out of range");
-        return SPGX_ERR_INVALID_ARG;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        return SPGX_ERR_CUDA;
     }
-    std::lock_guard<std::mutex> lock(mutex);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-            return SPGX_ERR_CUDA;
-        }
-        addr[dev] = static_cast<NoAllocScratch *>(p);
-    }
-    *out = addr[dev];
+    *out = static_cast<NoAllocScratch *>(p);
     return SPGX_OK;
 }
 
@@ -251,6 +250,11 @@ spgx_status spgx_eval_vertex_blocks_noalloc(int32_t type, int32_t n, const doubl
     }
     if (n < 0 || (n > 0 && (!X || !params || !slots || !grad || !hess))) {
         spgx::set_error("invalid argument");
+        return SPGX_ERR_INVALID_ARG;
+    }
+    if (S > spgx::kNoAllocMaxStencil || P > spgx::kNoAllocMaxParams) {
+        spgx::set_error("spgx_eval_vertex_blocks_noalloc: energy type " + std::to_string(type) +
+                        " has more stencil vertices or parameters than the fixed scratch array holds");
         return SPGX_ERR_INVALID_ARG;
     }
     if (n > spgx::kNoAllocMaxIncidences) {

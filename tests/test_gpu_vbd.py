@@ -14,20 +14,6 @@ def _f32(a):
     return np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
 
 
-def _incidence_samples(obj, rng, n_per_energy=300, jitter=0.0):
-    """(type, X, params, slot) samples from the object's own stencils at its current state."""
-    out = []
-    for e in obj.energies:
-        S = O.STENCIL_SIZE[e.type]
-        idx = rng.integers(0, e.n, size=min(n_per_energy, e.n))
-        for i in idx:
-            X = obj.x[e.stencils[i]].copy()
-            if jitter:
-                X += rng.normal(scale=jitter, size=X.shape)
-            out.append((e.type, _f32(X), _f32(e.params[i]), int(rng.integers(0, S))))
-    return out
-
-
 def _deformed(obj, steps, iters, dt=1 / 60):
     s = O.Vbd(obj, dt, 1, iters, scenes.GRAVITY, O.VERTEX_AD)
     for _ in range(steps):
@@ -37,35 +23,95 @@ def _deformed(obj, steps, iters, dt=1 / 60):
     return o
 
 
-@pytest.mark.parametrize("scene", ["cloth", "beam", "springs"])
-def test_element_blocks_match_tinyad_fp64(scene):
-    """GPU FP32 per-vertex gradient segments and Hessian blocks against the oracle's full
-    element AD (the reference's TinyAD path) on the same FP32 inputs: relative error 1e-5
-    (norm of the error over the norm of the FP64 value, per block)."""
-    rng = np.random.default_rng(7)
-    if scene == "cloth":
-        obj = _deformed(scenes.cloth_cfg1(17), 3, 20)
-    elif scene == "beam":
-        obj = _deformed(scenes.beam_cfg2(9, 4, 4), 3, 20)
-    else:
-        obj = _deformed(scenes.spring_cloth_cfg3(33), 3, 20, dt=1 / 120)
-    samples = _incidence_samples(obj, rng, jitter=2e-3 * float(np.ptp(obj.x)))
+U32 = 2.0 ** -24  # FP32 unit roundoff
+
+
+def _element_samples(obj, rng, positions, jitter_rel, n_per_energy=200):
+    """(type, X, params) of random elements of every energy, at `positions` moved by a random
+    displacement of relative size jitter_rel() of the element size."""
+    out = []
+    for e in obj.energies:
+        idx = rng.integers(0, e.n, size=min(n_per_energy, e.n))
+        for i in idx:
+            X = positions[e.stencils[i]].copy()
+            ell = max(float(np.ptp(X, axis=0).max()), 1e-3)
+            X += rng.normal(size=X.shape) * ell * jitter_rel()
+            out.append((e.type, _f32(X), _f32(e.params[i])))
+    return out
+
+
+def _element_errors(samples):
+    """Per energy type and element: every vertex block of the element on the GPU (FP32)
+    against the oracle's full-element FP64 AD (the reference's TinyAD path). Returns arrays of
+    eg = |g - g64| / |g64| over the element's whole gradient, egb = |g - g64| /
+    (1e-5 |g64| + 8 u |H64| l) (u the FP32 unit roundoff, l the element size) and
+    eh = |H_blocks - H64_blocks| / |H64| (Frobenius, the element's diagonal blocks against its
+    whole Hessian)."""
+    out = {}
     for etype in sorted({s[0] for s in samples}):
         sub = [s for s in samples if s[0] == etype]
-        X = np.stack([s[1].reshape(-1) for s in sub])
-        P = np.stack([s[2] for s in sub])
-        slots = np.array([s[3] for s in sub])
+        S = O.STENCIL_SIZE[etype]
+        X = np.repeat(np.stack([s[1].reshape(-1) for s in sub]), S, axis=0)
+        P = np.repeat(np.stack([s[2] for s in sub]), S, axis=0)
+        slots = np.tile(np.arange(S), len(sub))
         g, H = N.eval_vertex_blocks(etype, X, P, slots)
-        eg, eh = [], []
-        for k, (_, Xk, Pk, sl) in enumerate(sub):
-            gr, Hr = O.element_block(etype, Xk, Pk, sl, O.FULL_AD)
-            eg.append(np.linalg.norm(g[k] - gr) / max(np.linalg.norm(gr), 1e-300))
-            eh.append(np.linalg.norm(H[k] - Hr) / max(np.linalg.norm(Hr), 1e-300))
-        eg, eh = np.array(eg), np.array(eh)
-        print(f"{scene} type {etype}: grad rel err median {np.median(eg):.2e} p99 {np.quantile(eg, .99):.2e} "
-              f"max {eg.max():.2e}; hess median {np.median(eh):.2e} max {eh.max():.2e}")
-        assert np.median(eg) <= 1e-5 and np.median(eh) <= 1e-5
-        assert np.quantile(eh, 0.99) <= 1e-5
+        g = g.reshape(len(sub), 3 * S)
+        H = H.reshape(len(sub), S, 3, 3)
+        eg, egb, eh = [], [], []
+        for k, (_, Xk, Pk) in enumerate(sub):
+            gr, Hr = O.element_full(etype, Xk, Pk)
+            ell = float(np.ptp(Xk.reshape(-1, 3), axis=0).max()) if S > 1 else 1.0
+            d = np.linalg.norm(g[k] - gr)
+            nH = np.linalg.norm(Hr)
+            eg.append(d / max(np.linalg.norm(gr), 1e-300))
+            egb.append(d / max(1e-5 * np.linalg.norm(gr) + 8 * U32 * nH * ell, 1e-300))
+            dH = sum(np.linalg.norm(H[k, j] - Hr[3 * j:3 * j + 3, 3 * j:3 * j + 3]) ** 2 for j in range(S))
+            eh.append(np.sqrt(dH) / max(nH, 1e-300))
+        out[etype] = (np.array(eg), np.array(egb), np.array(eh))
+    return out
+
+
+def _scene(name):
+    if name == "cloth":
+        return scenes.cloth_cfg1(17), 1 / 60
+    if name == "beam":
+        return scenes.beam_cfg2(9, 4, 4), 1 / 60
+    return scenes.spring_cloth_cfg3(33), 1 / 120
+
+
+@pytest.mark.parametrize("scene", ["cloth", "beam", "springs"])
+def test_element_blocks_match_tinyad_fp64(scene):
+    """Per-element parity of the FP32 device blocks with the oracle's FP64 full-element AD on
+    the same FP32 inputs, every sampled element checked (the maximum, not a quantile), on
+    strained elements (the scene after 3 steps, jittered by 0.2 % of its extent) and near-rest
+    elements (rest positions moved by 1e-6 to 1e-2 of the element size).
+
+    - Hessians: the element's vertex blocks within 1e-5 of the element's Hessian (Frobenius).
+    - Springs and anchors: the element gradient within 1e-5 relative. The spring stretch
+      l - L0 is formed without cancellation, so this holds down to strains of 1e-6.
+    - Bending, StVK and Stable Neo-Hookean: their gradients vanish at rest, where an FP32
+      evaluation is a difference of terms of the size of |H| l (the FP32 dihedral angle alone
+      is resolved to about 1e-7 rad). They are held to 1e-5 relative plus 8 FP32 roundoffs of
+      that scale: |dg| <= 1e-5 |g| + 8 u |H| l, i.e. 1e-5 relative once the strain exceeds
+      about 5 %, and a few roundoffs of |H| l below it."""
+    rng = np.random.default_rng(7)
+    obj, dt = _scene(scene)
+    deformed = _deformed(obj, 3, 20, dt=dt)
+    extent_rel = 2e-3 * float(np.ptp(obj.x))
+    sets = {"strained": _element_samples(deformed, rng, deformed.x, lambda: 0.0),
+            "near-rest": _element_samples(obj, rng, obj.x0, lambda: 10.0 ** rng.uniform(-6, -2))}
+    # strained: the deformed scene plus an absolute jitter of 0.2 % of the extent
+    sets["strained"] = [(t, _f32(X + rng.normal(scale=extent_rel, size=X.shape)), p)
+                        for t, X, p in sets["strained"]]
+    for name, samples in sets.items():
+        for etype, (eg, egb, eh) in _element_errors(samples).items():
+            print(f"{scene} {name} type {etype}: element grad rel max {eg.max():.2e} (median {np.median(eg):.1e}), "
+                  f"bound use max {egb.max():.2f}; hess max {eh.max():.2e}")
+            assert eh.max() <= 1e-5
+            if etype in (O.SPRING, O.ANCHOR):
+                assert eg.max() <= 1e-5
+            else:
+                assert egb.max() <= 1.0
 
 
 @pytest.mark.parametrize("kernel", [1, 2, 3])
@@ -164,7 +210,8 @@ def test_colors_and_adjacency_through_handle():
     assert np.array_equal(c1, c2) and np.array_equal(e1, e2)
 
 
-@pytest.mark.parametrize("lanes,tile", [(1, 64), (2, 64), (4, 64), (4, 32), (2, 32), (4, 16), (8, 16)])
+@pytest.mark.parametrize("lanes,tile", [(1, 64), (2, 64), (4, 64), (4, 32), (2, 32), (4, 16), (8, 16), (3, 30),
+                                        (3, 40), (3, 32)])
 def test_dataflow_kernel_equals_colour_launches(lanes, tile):
     """The dataflow kernel runs the same Gauss-Seidel order as one launch per colour, so with
     the same lanes per vertex (same per-vertex summation order) it gives the same positions
@@ -174,7 +221,8 @@ def test_dataflow_kernel_equals_colour_launches(lanes, tile):
     kw = dict(dt=1 / 120, iterations=20, gravity=scenes.GRAVITY, lanes_per_vertex=lanes, tile_vertices=tile)
     a = N.VbdSolver([obj], kernel=2, **kw)
     b = N.VbdSolver([obj], kernel=3, **kw)
-    assert a.launch() == (2, lanes, tile * lanes) and b.launch() == (3, lanes, tile * lanes)
+    threads = tile * lanes if lanes != 3 else -(-tile // 10) * 32  # 3 lanes: warps of 10 vertices
+    assert a.launch() == (2, lanes, threads) and b.launch() == (3, lanes, threads)
     for _ in range(3):
         a.step()
         b.step()
@@ -197,8 +245,9 @@ def test_autotuned_tile_size(kernel):
     k, g, b = a.launch()
     if k == 1:
         pytest.skip("the lanes kernel won on this device")
-    assert k in (2, 3) and b // g in (32, 64) and b % g == 0
-    ref = N.VbdSolver([obj], kernel=k, lanes_per_vertex=g, tile_vertices=b // g, **kw)
+    tile = (b // 32) * 10 if g == 3 else b // g
+    assert k in (2, 3) and tile in ((30, 40) if g == 3 else (32, 64))
+    ref = N.VbdSolver([obj], kernel=k, lanes_per_vertex=g, tile_vertices=tile, **kw)
     assert ref.launch() == (k, g, b)
     for _ in range(3):
         a.step()
