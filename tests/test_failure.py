@@ -19,8 +19,7 @@ def test_dataflow_wait_runs_out_and_the_solver_recovers():
     s = N.VbdSolver([obj], **kw)
     k, g, b = s.launch()
     assert k == 3
-    tile = (b // 32) * 10 if g == 3 else b // g  # 3 lanes per vertex: warps of 10 vertices
-    twin = N.VbdSolver([obj], lanes_per_vertex=g, tile_vertices=tile, **kw)
+    twin = N.VbdSolver([obj], lanes_per_vertex=g, tile_vertices=b // g, **kw)
     assert twin.launch() == (k, g, b)
     s.step()
     twin.step()
