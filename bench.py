@@ -156,6 +156,18 @@ def algorithmic_bytes_per_iteration(obj) -> int:
     return 48 * nv + 4 * (nv + 1) + 4 * n_inc + sum(rec[e.type] * e.n for e in obj.energies)
 
 
+def xpbd_algorithmic_bytes_per_substep(obj) -> int:
+    """Compulsory bytes of one XPBD substep (one projection sweep over every stencil) in the
+    FP32 device layout: each stencil's record once (spring: indices, rest length, stiffness
+    16 B + compliance 4 B; bending: indices 16 B + angle, stiffness, compliance 16 B; anchor:
+    target and stiffness 16 B + compliance 8 B + vertex 4 B), and each vertex's state read and
+    written once (base and delta 32 B each way, velocity 16 B each way, the substep-start delta
+    and the inertial target 16 B each written, inverse mass 4 B read)."""
+    rec = {1: 20, 2: 28, 3: 32}
+    n = sum(rec.get(e.type, 0) * e.n for e in obj.energies)
+    return int(n + obj.nv * (32 + 32 + 16 + 16 + 16 + 16 + 4))
+
+
 def _measured_peaks() -> tuple[float, str]:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -327,11 +339,20 @@ def other_configs(local, only=None) -> dict:
         out["global_solvers_snh_beam_41x11x11"] = {"dt": "1/60 s (symplectic Euler 1e-4 s)", "precision": IMPLICIT_PRECISION,
                                                    "solvers": solvers}
     if want("xpbd_spring_cloth_513_20substeps"):
-        x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local)
-        ms = statistics.mean(_timed_steps(x, 5))
-        out["xpbd_spring_cloth_513_20substeps"] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
-                                                   "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3)}
-        x.close()
+        peak, peak_kind = _measured_peaks()
+        alg = xpbd_algorithmic_bytes_per_substep(big)
+        entry = {}
+        for kernel, name in ((2, "dataflow"), (1, "phase_launches")):
+            x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local, kernel=kernel)
+            ms = statistics.mean(_timed_steps(x, 5))
+            achieved = alg * 20 / (ms * 1e-3) / 1e9
+            entry[name] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
+                           "vertex_substeps_per_s": big.nv * 20 / (ms * 1e-3),
+                           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                        "frac": achieved / peak, "peak_source": peak_kind,
+                                        "algorithmic_bytes_per_substep": alg}}
+            x.close()
+        out["xpbd_spring_cloth_513_20substeps"] = entry
     if want("mesh_input"):
         out["mesh_input"] = mesh_input()
     if want("topology_change"):

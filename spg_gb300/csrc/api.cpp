@@ -75,6 +75,7 @@ void spgx_xpbd_params_default(spgx_xpbd_params *p)
     p->block_size = 0;
     p->use_graph = 1;
     p->device = 0;
+    p->kernel = 0;
 }
 
 }  // extern "C"

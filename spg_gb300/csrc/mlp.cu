@@ -1,10 +1,10 @@
 // Per-vertex MLP of the learned warm start: 24 -> 128 -> 128 -> 128 -> 3 with GELU, BF16
 // weights, FP32 accumulation.
 //
-// Inference (mlp_infer_kernel) runs on the tensor cores with mma.sync m16n8k16 BF16: each warp
-// owns 16 rows, the weights of all four layers are staged in shared memory as BF16 (transposed so
-// each B fragment register is one 32-bit load), and the FP32 accumulator fragments of one layer
-// become, after bias and GELU, the BF16 A fragments of the next without leaving registers.
+// Inference (mlp_infer_tc_kernel) runs on the 5th-generation tensor cores: tcgen05.mma with
+// BF16 operands in shared memory and the FP32 accumulator in tensor memory, one 128-row tile
+// per CTA at a time; each layer's accumulator is read back with tcgen05.ld, biased, passed
+// through GELU and rounded to BF16 as the next layer's operand.
 //
 // Training runs FP32 SIMT kernels (a tiled GEMM, GELU forward/backward, bias reductions, Adam)
 // on FP32 master weights whose BF16 rounding is used in the forward pass, so the trained
@@ -54,9 +54,6 @@ struct MlpDevWeights {
     const float *b1, *b2, *b3, *b4;  // 128, 128, 128, 8
 };
 
-constexpr int kInferThreads = 256;  // 8 warps x 16 rows
-constexpr size_t kInferSmem = size_t(128 * 32 + 128 * 128 * 2 + 8 * 128) * 2 + size_t(128 * 3 + 8) * 4;
-
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -65,125 +62,264 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return r;
 }
 
-__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, uint32_t b0, uint32_t b1)
+// ---------------------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05): a persistent kernel over tiles of
+// 128 rows. Per tile and layer one thread issues the layer's tcgen05.mma instructions
+// (M = 128 rows, N = 128 hidden units or 16 for the padded 3 outputs, K = 16 per
+// instruction, BF16 operands from shared memory, FP32 accumulator in tensor memory) and
+// commits them to an mbarrier; the four warps then read the accumulator rows back with
+// tcgen05.ld (warp w owns tensor-memory lanes 32w..32w+31, one row per thread), add the bias,
+// apply GELU, round to BF16 and write the next layer's A operand into shared memory.
+//
+// Shared-memory operands use the K-major layout without swizzle: 8 x 8 BF16 core matrices
+// of 128 contiguous bytes (8 rows of 16 bytes); core matrices adjacent along K are 128 bytes
+// apart (the descriptor's leading byte offset) and adjacent 8-row groups K / 8 * 128 bytes
+// apart (its stride byte offset).
+namespace tc {
+
+constexpr int kRows = 128;
+constexpr int kThreads = 128;
+constexpr int kW1 = 0;                       // W1^T: 128 x 32 (K padded 24 -> 32)
+constexpr int kW2 = kW1 + 128 * 32 * 2;      // W2^T: 128 x 128
+constexpr int kW3 = kW2 + 128 * 128 * 2;     // W3^T: 128 x 128
+constexpr int kW4 = kW3 + 128 * 128 * 2;     // W4^T: 16 x 128 (N padded 3 -> 16)
+constexpr int kA = kW4 + 16 * 128 * 2;       // activations: 128 x 128 (layer 1: 128 x 32)
+constexpr int kBias = kA + 128 * 128 * 2;    // b1, b2, b3 (128 each), b4 (16)
+constexpr int kBar = kBias + (3 * 128 + 16) * 4;
+constexpr int kTmemSlot = kBar + 8;
+constexpr size_t kSmem = size_t(kTmemSlot + 8) + 1024;  // + slack to align the base to 1 KB
+constexpr int kTmemCols = 128;
+constexpr int kMaxPolls = 1 << 22;
+
+// Byte offset of element (r, k) of a K-major operand with K columns, in core matrices.
+__device__ __forceinline__ int core_off(int r, int k, int K)
+{
+    return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// Shared-memory matrix descriptor: start address, leading byte offset (K direction), stride
+// byte offset (8-row groups), descriptor version 1 (bits 46-47), no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return uint64_t((addr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits
+// 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
 {
     asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
-// One hidden layer: acc[16 n-tiles][4] = A (16 x K, as KS k-step fragments) * W (K x 128).
-template <int KS>
-__device__ __forceinline__ void mma_layer(float (*acc)[4], const uint32_t (*a)[4], const __nv_bfloat16 *wt, int ldk,
-                                          int gid, int tid4)
+__device__ __forceinline__ void commit(uint32_t bar)
 {
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-        const __nv_bfloat16 *row = wt + (j * 8 + gid) * ldk + tid4 * 2;
-#pragma unroll
-        for (int s = 0; s < KS; ++s) {
-            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + s * 16);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + s * 16 + 8);
-            mma_bf16(acc[j], a[s], b0, b1);
-        }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+// Bounded wait for the mbarrier phase `parity` to complete; false when the polls run out.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < kMaxPolls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (i > 64) __nanosleep(64);
     }
+    return false;
 }
 
-// Bias + GELU on a layer's accumulators and repacking as the next layer's A fragments.
-__device__ __forceinline__ void activate(float (*acc)[4], uint32_t (*a)[4], const float *bias, int tid4)
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// Shared-memory writes by the threads, made visible to the tensor cores' (async-proxy) reads.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// 32 consecutive FP32 accumulator columns of this thread's row (tensor-memory lane).
+__device__ __forceinline__ void ld32(uint32_t taddr, float *v)
 {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const int j0 = 2 * s, j1 = 2 * s + 1;
-        const float bA0 = bias[j0 * 8 + tid4 * 2], bA1 = bias[j0 * 8 + tid4 * 2 + 1];
-        const float bB0 = bias[j1 * 8 + tid4 * 2], bB1 = bias[j1 * 8 + tid4 * 2 + 1];
-        a[s][0] = pack_bf16(gelu(acc[j0][0] + bA0), gelu(acc[j0][1] + bA1));
-        a[s][1] = pack_bf16(gelu(acc[j0][2] + bA0), gelu(acc[j0][3] + bA1));
-        a[s][2] = pack_bf16(gelu(acc[j1][0] + bB0), gelu(acc[j1][1] + bB1));
-        a[s][3] = pack_bf16(gelu(acc[j1][2] + bB0), gelu(acc[j1][3] + bB1));
-    }
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__global__ void __launch_bounds__(kInferThreads) mlp_infer_kernel(MlpDevWeights W, const float *__restrict__ X, int n,
-                                                                  float *__restrict__ Y)
+__device__ __forceinline__ void ld16(uint32_t taddr, float *v)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __nv_bfloat16 *s_w1 = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
-    __nv_bfloat16 *s_w2 = s_w1 + 128 * 32;
-    __nv_bfloat16 *s_w3 = s_w2 + 128 * 128;
-    __nv_bfloat16 *s_w4 = s_w3 + 128 * 128;
-    float *s_b = reinterpret_cast<float *>(s_w4 + 8 * 128);
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(tc::kThreads) mlp_infer_tc_kernel(MlpDevWeights W, const float *__restrict__ X,
+                                                                    int n, float *__restrict__ Y,
+                                                                    unsigned int *status)
+{
+    extern __shared__ unsigned char smem_raw[];
+    // The operand region starts on a 1 KB boundary.
+    unsigned char *sm = smem_raw + ((1024 - (static_cast<uint32_t>(__cvta_generic_to_shared(smem_raw)) & 1023)) & 1023);
+    const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(sm));
+    float *s_b = reinterpret_cast<float *>(sm + tc::kBias);
+    const uint32_t bar = sbase + tc::kBar;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + tc::kTmemSlot);
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    // Weights into the core-matrix layout, 16 bytes (8 consecutive k of one row n) per copy.
     {
-        const uint4 *src[4] = {reinterpret_cast<const uint4 *>(W.w1t), reinterpret_cast<const uint4 *>(W.w2t),
-                               reinterpret_cast<const uint4 *>(W.w3t), reinterpret_cast<const uint4 *>(W.w4t)};
-        uint4 *dst[4] = {reinterpret_cast<uint4 *>(s_w1), reinterpret_cast<uint4 *>(s_w2),
-                         reinterpret_cast<uint4 *>(s_w3), reinterpret_cast<uint4 *>(s_w4)};
-        const int cnt[4] = {128 * 32 / 8, 128 * 128 / 8, 128 * 128 / 8, 8 * 128 / 8};
+        const int K[4] = {32, 128, 128, 128}, Nr[4] = {128, 128, 128, 16}, off[4] = {tc::kW1, tc::kW2, tc::kW3, tc::kW4};
+        const __nv_bfloat16 *src[4] = {W.w1t, W.w2t, W.w3t, W.w4t};
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-            for (int i = threadIdx.x; i < cnt[m]; i += blockDim.x) dst[m][i] = __ldg(src[m] + i);
-        for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+        for (int m = 0; m < 4; ++m) {
+            const int chunks = Nr[m] * K[m] / 8;
+            for (int i = tid; i < chunks; i += blockDim.x) {
+                const int nn = i / (K[m] / 8), k = (i % (K[m] / 8)) * 8;
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (m < 3 || nn < 8) v = __ldg(reinterpret_cast<const uint4 *>(src[m] + nn * K[m] + k));
+                *reinterpret_cast<uint4 *>(sm + off[m] + tc::core_off(nn, k, K[m])) = v;
+            }
+        }
+        for (int i = tid; i < 128; i += blockDim.x) {
             s_b[i] = W.b1[i];
             s_b[128 + i] = W.b2[i];
             s_b[256 + i] = W.b3[i];
         }
-        if (threadIdx.x < 8) s_b[384 + threadIdx.x] = W.b4[threadIdx.x];
+        if (tid < 16) s_b[384 + tid] = tid < 8 ? W.b4[tid] : 0.f;
     }
+    if (warp == 0) {
+        const uint32_t slot = static_cast<uint32_t>(__cvta_generic_to_shared(tmem_slot));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(slot),
+                     "r"(tc::kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    tc::fence_async_smem();
+    tc::fence_before();
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int gid = lane >> 2, tid4 = lane & 3;
-    const int tiles = (n + 15) / 16;
-    for (int t = blockIdx.x * (kInferThreads / 32) + warp; t < tiles; t += gridDim.x * (kInferThreads / 32)) {
-        const int r0 = t * 16 + gid, r1 = r0 + 8;
-        // Layer-1 A fragments straight from the FP32 features (k padded to 32 with zeros).
-        uint32_t a[8][4];
+    tc::fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_base = uint32_t(warp * 32) << 16;  // this warp's tensor-memory lanes
+    uint32_t phase = 0;
+    bool ok = true;
+    const int tiles = (n + tc::kRows - 1) / tc::kRows;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        const int row = t * tc::kRows + tid;
+        // Layer-1 operand: the 24 features of this thread's row as BF16, K padded to 32.
+        {
+            float f[32];
 #pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            float v[8];
+            for (int k = 0; k < 32; ++k) f[k] = 0.f;
+            if (row < n) {
+                const float4 *xr = reinterpret_cast<const float4 *>(X + size_t(row) * 24);
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int k0 = s * 16 + q * 8 + tid4 * 2;
-                v[4 * q + 0] = (r0 < n && k0 < 24) ? X[size_t(r0) * 24 + k0] : 0.f;
-                v[4 * q + 1] = (r0 < n && k0 + 1 < 24) ? X[size_t(r0) * 24 + k0 + 1] : 0.f;
-                v[4 * q + 2] = (r1 < n && k0 < 24) ? X[size_t(r1) * 24 + k0] : 0.f;
-                v[4 * q + 3] = (r1 < n && k0 + 1 < 24) ? X[size_t(r1) * 24 + k0 + 1] : 0.f;
+                for (int q = 0; q < 6; ++q) {
+                    const float4 v = __ldg(xr + q);
+                    f[4 * q] = v.x, f[4 * q + 1] = v.y, f[4 * q + 2] = v.z, f[4 * q + 3] = v.w;
+                }
             }
-            a[s][0] = pack_bf16(v[0], v[1]);
-            a[s][1] = pack_bf16(v[2], v[3]);
-            a[s][2] = pack_bf16(v[4], v[5]);
-            a[s][3] = pack_bf16(v[6], v[7]);
-        }
-        float acc[16][4];
-        mma_layer<2>(acc, a, s_w1, 32, gid, tid4);
-        activate(acc, a, s_b, tid4);
-        mma_layer<8>(acc, a, s_w2, 128, gid, tid4);
-        activate(acc, a, s_b + 128, tid4);
-        mma_layer<8>(acc, a, s_w3, 128, gid, tid4);
-        activate(acc, a, s_b + 256, tid4);
-        float out[4] = {0.f, 0.f, 0.f, 0.f};
-        const __nv_bfloat16 *row = s_w4 + gid * 128 + tid4 * 2;
 #pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(row + s * 16);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(row + s * 16 + 8);
-            mma_bf16(out, a[s], b0, b1);
+            for (int k = 0; k < 32; k += 8) {
+                const uint4 v = make_uint4(pack_bf16(f[k], f[k + 1]), pack_bf16(f[k + 2], f[k + 3]),
+                                           pack_bf16(f[k + 4], f[k + 5]), pack_bf16(f[k + 6], f[k + 7]));
+                *reinterpret_cast<uint4 *>(sm + tc::kA + tc::core_off(tid, k, 32)) = v;
+            }
         }
-        const int c0 = tid4 * 2;
-        if (c0 < 3) {
-            if (r0 < n) Y[size_t(r0) * 3 + c0] = out[0] + s_b[384 + c0];
-            if (r1 < n) Y[size_t(r1) * 3 + c0] = out[2] + s_b[384 + c0];
-        }
-        if (c0 + 1 < 3) {
-            if (r0 < n) Y[size_t(r0) * 3 + c0 + 1] = out[1] + s_b[384 + c0 + 1];
-            if (r1 < n) Y[size_t(r1) * 3 + c0 + 1] = out[3] + s_b[384 + c0 + 1];
+        for (int layer = 0; layer < 4; ++layer) {
+            const int K = layer == 0 ? 32 : 128, N = layer == 3 ? 16 : 128;
+            const int woff = layer == 0 ? tc::kW1 : layer == 1 ? tc::kW2 : layer == 2 ? tc::kW3 : tc::kW4;
+            tc::fence_async_smem();
+            tc::fence_before();
+            __syncthreads();  // the operand is written and every read of the accumulator is done
+            tc::fence_after();
+            if (tid == 0) {
+                const uint32_t idesc = tc::idesc_bf16(128, N);
+                for (int ks = 0; ks < K / 16; ++ks) {
+                    const uint64_t a = tc::smem_desc(sbase + tc::kA + ks * 256, 128, (K / 8) * 128);
+                    const uint64_t b = tc::smem_desc(sbase + woff + ks * 256, 128, (K / 8) * 128);
+                    tc::mma(tmem, a, b, idesc, ks > 0 ? 1u : 0u);
+                }
+                tc::commit(bar);
+            }
+            ok = __syncthreads_and(tc::wait_phase(bar, phase));  // the same verdict in every thread
+            phase ^= 1u;
+            tc::fence_after();
+            if (!ok) break;
+            if (layer < 3) {
+                const float *bias = s_b + layer * 128;
+#pragma unroll 1
+                for (int c0 = 0; c0 < 128; c0 += 32) {
+                    float v[32];
+                    tc::ld32(tmem + lane_base + uint32_t(c0), v);
+#pragma unroll
+                    for (int k = 0; k < 32; k += 8) {
+                        float g[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) g[q] = gelu(v[k + q] + bias[c0 + k + q]);
+                        const uint4 o = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]),
+                                                   pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
+                        *reinterpret_cast<uint4 *>(sm + tc::kA + tc::core_off(tid, c0 + k, 128)) = o;
+                    }
+                }
+            } else {
+                float v[16];
+                tc::ld16(tmem + lane_base, v);
+                if (row < n) {
+                    Y[size_t(row) * 3 + 0] = v[0] + s_b[384 + 0];
+                    Y[size_t(row) * 3 + 1] = v[1] + s_b[384 + 1];
+                    Y[size_t(row) * 3 + 2] = v[2] + s_b[384 + 2];
+                }
+            }
         }
     }
+    if (!ok) {
+        // A commit that never arrived: record it, and give the tensor cores a bounded while to
+        // finish before the tensor memory is released.
+        if (tid == 0) atomicOr(status, 1u);
+        tc::wait_phase(bar, phase ^ 1u);
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tc::kTmemCols)
+                     : "memory");
 }
 
-// BF16 transposed copies of the FP32 master weights for the inference kernel.
+// BF16 transposed copies of the FP32 master weights for the inference kernel (row n of W^T
+// holds the K inputs of output n; W4 is padded to 8 rows and W1 to K = 32).
 __global__ void mlp_pack_kernel(const float *__restrict__ w, __nv_bfloat16 *w1t, __nv_bfloat16 *w2t,
                                 __nv_bfloat16 *w3t, __nv_bfloat16 *w4t, float *b4pad)
 {
@@ -359,8 +495,11 @@ spgx_status Mlp::init(uint64_t seed, int dev)
     SPGX_TRY_STATUS(d_w4t.alloc(8 * 128 * 2));
     SPGX_TRY_STATUS(d_b4.alloc(8 * sizeof(float)));
     SPGX_TRY_STATUS(d_loss.alloc(sizeof(double)));
-    SPGX_CUDA(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(kInferSmem)));
+    SPGX_CUDA(cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(tc::kSmem)));
+    SPGX_TRY_STATUS(d_status.alloc(sizeof(unsigned int)));
+    SPGX_CUDA(cudaMemset(d_status.as<void>(), 0, sizeof(unsigned int)));
+    SPGX_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
     // Xavier-uniform initialisation, zero biases.
     std::vector<float> w(kMlpParams, 0.f);
     std::mt19937_64 rng(seed);
@@ -410,9 +549,21 @@ void Mlp::infer(const float *X, int n, float *Y, cudaStream_t st) const
     MlpDevWeights W{d_w1t.as<__nv_bfloat16>(), d_w2t.as<__nv_bfloat16>(), d_w3t.as<__nv_bfloat16>(),
                     d_w4t.as<__nv_bfloat16>(), d_w.as<float>() + kMlpOffB1, d_w.as<float>() + kMlpOffB2,
                     d_w.as<float>() + kMlpOffB3, d_b4.as<float>()};
-    const int tiles = (n + 15) / 16;
-    const int grid = std::min(std::max(1, (tiles + 7) / 8), 2 * 152);
-    mlp_infer_kernel<<<grid, kInferThreads, kInferSmem, st>>>(W, X, n, Y);
+    const int tiles = (n + tc::kRows - 1) / tc::kRows;
+    const int grid = std::min(tiles, 2 * std::max(1, num_sms));  // two 110 KB CTAs per SM
+    mlp_infer_tc_kernel<<<grid, tc::kThreads, tc::kSmem, st>>>(W, X, n, Y, d_status.as<unsigned int>());
+}
+
+spgx_status Mlp::take_status()
+{
+    unsigned int hs = 0;
+    SPGX_CUDA(cudaMemcpy(&hs, d_status.as<void>(), sizeof(hs), cudaMemcpyDeviceToHost));
+    if (hs & 1u) {
+        SPGX_CUDA(cudaMemset(d_status.as<void>(), 0, sizeof(unsigned int)));
+        set_error("MLP inference gave up waiting for the tensor cores (bounded wait)");
+        return SPGX_ERR_TIMEOUT;
+    }
+    return SPGX_OK;
 }
 
 spgx_status Mlp::ensure_batch(int M)
@@ -603,7 +754,7 @@ spgx_status spgx_mlp_forward(spgx_mlp *h, int32_t n, const float *x, float *y)
     SPGX_CUDA(cudaGetLastError());
     SPGX_CUDA(cudaMemcpyAsync(y, dy.as<float>(), size_t(n) * 3 * sizeof(float), cudaMemcpyDeviceToHost, h->m->stream));
     SPGX_CUDA(cudaStreamSynchronize(h->m->stream));
-    return SPGX_OK;
+    return h->m->take_status();
     SPGX_GUARD_END
 }
 

@@ -30,6 +30,8 @@ struct Mlp {
     DevBuf d_w, d_wq, d_g, d_m, d_v;         // master weights, BF16-rounded copy, grad, Adam moments
     DevBuf d_w1t, d_w2t, d_w3t, d_w4t, d_b4;  // BF16 transposed copies for inference
     DevBuf d_loss;
+    DevBuf d_status;  // bit 0: an inference tile's tensor-core commit never arrived (bounded wait)
+    int num_sms{0};
     DevBuf z1, a1, z2, a2, z3, a3, yb, dy, da, db_, xb, tb, ib;
     int batch_cap{0};
     long adam_t{0};
@@ -47,8 +49,12 @@ struct Mlp {
     spgx_status loss_grad_device(const float *X, const float *T, int M, double *loss_out);
     spgx_status train(const float *X, const float *T, int n, int steps, int batch, float lr, uint64_t seed,
                       float *final_loss);
-    // Y (n x 3) = MLP(X (n x 24)) on the tensor cores, both device pointers, on stream st.
+    // Y (n x 3) = MLP(X (n x 24)) on the tensor cores (tcgen05), both device pointers (X 16-byte
+    // aligned), on stream st.
     void infer(const float *X, int n, float *Y, cudaStream_t st) const;
+    // SPGX_ERR_TIMEOUT (and the flag cleared) when an inference since the last call gave up
+    // waiting for the tensor cores; call after synchronising the stream the inference ran on.
+    spgx_status take_status();
 };
 
 }  // namespace spgx

@@ -58,7 +58,8 @@ class VbdParams(C.Structure):
 
 class XpbdParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("substeps", C.c_int32), ("gravity", C.c_double * 3),
-                ("block_size", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32)]
+                ("block_size", C.c_int32), ("use_graph", C.c_int32), ("device", C.c_int32),
+                ("kernel", C.c_int32)]
 
 
 class ImplicitParams(C.Structure):
@@ -120,6 +121,7 @@ def lib():
         L.spgx_xpbd_set_state.argtypes = [vp, i32, dp, dp]
         L.spgx_xpbd_reset.argtypes = [vp]
         L.spgx_xpbd_get_stencil_colors.argtypes = [vp, i32, i32, ip]
+        L.spgx_xpbd_test_stall.argtypes = [vp]
         L.spgx_color_vertices.argtypes = [C.POINTER(ObjectDesc), ip]
         L.spgx_color_stencils.argtypes = [C.POINTER(EnergyDesc), ip]
         L.spgx_incidences.argtypes = [C.POINTER(ObjectDesc), ip, ip, C.POINTER(C.c_int64)]
@@ -464,7 +466,8 @@ class ImplicitSolver:
 
 
 class XpbdSolver:
-    def __init__(self, objects, dt=0.01, substeps=1, gravity=(0.0, -9.8, 0.0), block_size=0, use_graph=1, device=0):
+    def __init__(self, objects, dt=0.01, substeps=1, gravity=(0.0, -9.8, 0.0), block_size=0, use_graph=1, device=0,
+                 kernel=0):
         self.objects_nv = [len(np.asarray(o.mass).reshape(-1)) for o in objects]
         self.n_stencils = [[len(np.asarray(e.stencils).reshape(-1)) // STENCIL_SIZE[e.type] for e in o.energies]
                            for o in objects]
@@ -473,7 +476,7 @@ class XpbdSolver:
         lib().spgx_xpbd_params_default(C.byref(p))
         p.dt, p.substeps = dt, substeps
         p.gravity = (C.c_double * 3)(*gravity)
-        p.block_size, p.use_graph, p.device = block_size, use_graph, device
+        p.block_size, p.use_graph, p.device, p.kernel = block_size, use_graph, device, kernel
         self.params = p
         h = C.c_void_p()
         check(lib().spgx_xpbd_create(C.byref(self._d.scene), C.byref(p), C.byref(h)))
@@ -502,6 +505,10 @@ class XpbdSolver:
         x = np.ascontiguousarray(x, dtype=np.float64)
         vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         check(lib().spgx_xpbd_set_state(self.h, obj, _p(x, C.c_double), None if vv is None else _p(vv, C.c_double)))
+
+    def test_stall(self):
+        """Failure-detection test hook: the next dataflow step's waits on one chunk run out."""
+        check(lib().spgx_xpbd_test_stall(self.h))
 
     def stencil_colors(self, obj, energy):
         out = np.zeros(self.n_stencils[obj][energy], np.int32)

@@ -48,3 +48,29 @@ def test_stall_hook_needs_the_dataflow_kernel():
     s = N.VbdSolver([obj], dt=1 / 120, iterations=1, gravity=scenes.GRAVITY, kernel=1)
     with pytest.raises(N.SpgxError):
         s.test_stall_tile(0)
+
+
+def test_xpbd_dataflow_wait_runs_out_and_the_solver_recovers():
+    """The XPBD dataflow kernel's bounded waits: a chunk counter that no substep reaches makes
+    the step return a timeout status; restored to the state before that step, the handle steps
+    exactly like a twin that never stalled."""
+    obj = scenes.spring_cloth_cfg3(65)
+    kw = dict(dt=1 / 120, substeps=10, gravity=scenes.GRAVITY, kernel=2)
+    s = N.XpbdSolver([obj], **kw)
+    twin = N.XpbdSolver([obj], **kw)
+    s.step()
+    twin.step()
+    x0, v0 = s.state(0)
+    twin.set_state(0, *twin.state(0))
+    s.test_stall()
+    t0 = time.time()
+    with pytest.raises(N.SpgxError) as err:
+        s.step()
+    elapsed = time.time() - t0
+    assert err.value.status == SPGX_ERR_TIMEOUT, err.value
+    assert elapsed < 30, elapsed
+    s.set_state(0, x0, v0)
+    s.step()
+    twin.step()
+    assert np.array_equal(s.state(0)[0], twin.state(0)[0])
+    print(f"stalled XPBD step returned after {elapsed:.2f} s")

@@ -88,14 +88,16 @@ def test_loss_gradient_matches_oracle():
 
 @pytest.mark.gpu
 def test_tensor_core_inference_matches_oracle():
-    """BF16 mma.sync inference against the oracle evaluated with the kernel's BF16 operand
-    rounding (inputs and hidden activations) and FP64 accumulation. The tolerance covers FP32
-    accumulation order and an occasional one-ulp difference of a rounded activation."""
+    """tcgen05 BF16 inference (FP32 accumulator in tensor memory) against the oracle evaluated
+    with the kernel's BF16 operand rounding (inputs and hidden activations) and FP64
+    accumulation. The tolerance covers FP32 accumulation order and an occasional one-ulp
+    difference of a rounded activation. 100003 rows are more 128-row tiles than the grid has
+    CTAs, so each CTA runs several tiles through the same tensor memory and mbarrier."""
     rng = np.random.default_rng(4)
     mlp = N.Mlp(seed=5)
     w = _weights(rng)
     mlp.set_weights(w)
-    for n in (1, 15, 17, 4096 + 5):
+    for n in (1, 15, 17, 128, 129, 4096 + 5, 100003):
         x = _features(rng, n)
         y = mlp.forward(x)
         ref = M.forward(w, x, emulate_bf16_activations=True)
