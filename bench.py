@@ -353,6 +353,20 @@ def other_configs(local, only=None) -> dict:
                                         "algorithmic_bytes_per_substep": alg}}
             x.close()
         out["xpbd_spring_cloth_513_20substeps"] = entry
+    if want("mlp_inference_spring_cloth_513"):
+        # The learned warm start's network on every vertex of the 513x513 cloth: host arrays in
+        # and out through the C ABI (the kernel's own time is in the ncu launch list).
+        from spg_gb300 import warm_start as WS
+        rng = np.random.default_rng(0)
+        x = rng.standard_normal((ROWS * ROWS, 24)).astype(np.float32)
+        mlp = WS.load_mlp(local) if os.path.exists(WS.WEIGHTS) else N.Mlp(seed=1, device=local)
+        mlp.forward(x)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            mlp.forward(x)
+        out["mlp_inference_spring_cloth_513"] = {"rows": ROWS * ROWS, "ms_per_call_with_copies":
+                                                 1e3 * (time.perf_counter() - t0) / 5}
+        mlp.close()
     if want("mesh_input"):
         out["mesh_input"] = mesh_input()
     if want("topology_change"):

@@ -49,8 +49,9 @@ typedef enum spgx_energy_type {
     SPGX_ENERGY_DISCRETE_BENDING = 3,   /* spg::DiscreteBendingEnergy    discreteBendingEnergy.h:9 */
     SPGX_ENERGY_MEMBRANE_STVK = 4,      /* spg::MembraneStvkEnergy       membraneStvkEnergy.h:9 */
     SPGX_ENERGY_STABLE_NEO_HOOKEAN = 5, /* spg::StableNeoHookeanEnergy   stableNeoHookeanEnergy.h:10 */
-    /* The types below run on the lanes-per-vertex kernel (kernel 1) with per-vertex forward-mode
-     * derivatives on the device, and are not accepted by the XPBD solver. */
+    /* The types below take their per-vertex blocks from forward-mode derivatives on the device
+     * (every VBD kernel); XPBD accepts 6-13 (the static load has no constraint form, and the
+     * reference throws for it too). */
     SPGX_ENERGY_STVK = 6,                         /* spg::StvkEnergy (tet)              stvkEnergy.h */
     SPGX_ENERGY_STABLE_SQUARED_NEO_HOOKEAN = 7,   /* spg::StableSquaredNeoHookeanEnergy */
     SPGX_ENERGY_MEMBRANE_BARAFF_WITKIN = 8,       /* spg::MembraneBaraffWitkinEnergy */

@@ -34,6 +34,18 @@ __device__ __forceinline__ float gelu(float x)
     return 0.5f * x * (1.f + tanhf(u));
 }
 
+// The same GELU with the hardware's approximate tanh (PTX tanh.approx.f32, one instruction;
+// its error, about 2^-11 relative, is below the BF16 rounding the inference kernel applies to
+// every activation). The tcgen05 kernel's epilogue is bound by this function: with tanhf it
+// took 136 us on 263k rows, with the hardware tanh 92 us.
+__device__ __forceinline__ float gelu_fast(float x)
+{
+    const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+    return 0.5f * x * (1.f + t);
+}
+
 __device__ __forceinline__ float gelu_grad(float x)
 {
     const float x2 = x * x;
@@ -69,7 +81,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 // instruction, BF16 operands from shared memory, FP32 accumulator in tensor memory) and
 // commits them to an mbarrier; the four warps then read the accumulator rows back with
 // tcgen05.ld (warp w owns tensor-memory lanes 32w..32w+31, one row per thread), add the bias,
-// apply GELU, round to BF16 and write the next layer's A operand into shared memory.
+// apply GELU (gelu_fast), round to BF16 and write the next layer's A operand into shared
+// memory.
 //
 // Shared-memory operands use the K-major layout without swizzle: 8 x 8 BF16 core matrices
 // of 128 contiguous bytes (8 rows of 16 bytes); core matrices adjacent along K are 128 bytes
@@ -287,7 +300,7 @@ __global__ void __launch_bounds__(tc::kThreads) mlp_infer_tc_kernel(MlpDevWeight
                     for (int k = 0; k < 32; k += 8) {
                         float g[8];
 #pragma unroll
-                        for (int q = 0; q < 8; ++q) g[q] = gelu(v[k + q] + bias[c0 + k + q]);
+                        for (int q = 0; q < 8; ++q) g[q] = gelu_fast(v[k + q] + bias[c0 + k + q]);
                         const uint4 o = make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]),
                                                    pack_bf16(g[4], g[5]), pack_bf16(g[6], g[7]));
                         *reinterpret_cast<uint4 *>(sm + tc::kA + tc::core_off(tid, c0 + k, 128)) = o;

@@ -21,7 +21,11 @@ struct Incidence {
     int slot;
 };
 
-constexpr int kRecordUnits[kNumClasses] = {1, 1, 1, 1, 3, 4};
+// Energies of types 6-14 follow the six classes in a vertex's record block, one unit each:
+// {local v0 | v1 << 16, local v2 | v3 << 16, type | slot << 8 | stencil size << 16,
+// parameter offset in the generic parameter table}.
+constexpr int kClsGeneric = kNumClasses;
+constexpr int kRecordUnits[kNumClasses + 1] = {1, 1, 1, 1, 3, 4, 1};
 
 // Vertices read by one incidence other than its own vertex.
 int others(const ElementTables &T, const Incidence &inc, int self, int *out)
@@ -44,6 +48,13 @@ int others(const ElementTables &T, const Incidence &inc, int self, int *out)
         push(s.x), push(s.y), push(s.z);
         break;
     }
+    case kClsGeneric: {
+        const I4 &s = T.gen_idx[inc.elem];
+        const int S = T.gen_info[inc.elem].z;
+        const int all[4] = {s.x, s.y, s.z, s.w};
+        for (int j = 0; j < S; ++j) push(all[j]);
+        break;
+    }
     default: {
         const I4 &s = T.snh_idx[inc.elem];
         push(s.x), push(s.y), push(s.z), push(s.w);
@@ -62,6 +73,8 @@ void incidences(const SceneLayout &L, int v, std::vector<Incidence> &list)
     int off = h.x;
     for (int c = 0; c < kNumClasses; ++c)
         for (int k = 0; k < cnt[c]; ++k, ++off) list.push_back({c, L.adj[off] >> 2, L.adj[off] & 3});
+    if (!L.gen_off.empty())
+        for (int k = L.gen_off[v]; k < L.gen_off[v + 1]; ++k) list.push_back({kClsGeneric, L.gen_adj[k] >> 2, L.gen_adj[k] & 3});
 }
 
 int record_units(const std::vector<Incidence> &list)
@@ -108,6 +121,15 @@ void emit(const ElementTables &T, const Incidence &i, const std::vector<int32_t>
         out.push_back({local[s.x] | (local[s.y] << 16), local[s.z] | (i.slot << 16), fb(D.x), fb(D.y)});
         out.push_back({fb(D.z), fb(D.w), fb(Ka.x), fb(Ka.y)});
         out.push_back({fb(Ka.z), fb(Ka.w), fb(Kb.x), fb(Kb.y)});
+        break;
+    }
+    case kClsGeneric: {
+        const I4 &s = T.gen_idx[i.elem];
+        const I4 &info = T.gen_info[i.elem];
+        const int S = info.z;
+        auto loc = [&](int j, int v) { return j < S ? local[v] : 0; };
+        out.push_back({loc(0, s.x) | (loc(1, s.y) << 16), loc(2, s.z) | (loc(3, s.w) << 16),
+                       info.x | (i.slot << 8) | (S << 16), info.y});
         break;
     }
     default: {

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) vbd_color_kernel(const DevTables T, const
 
 // One colour phase with the shared-memory tile kernel: one CTA per tile of the colour,
 // G lanes per tile vertex (blockDim = tile_vertices * G).
-template <int G>
+template <int G, bool kGeneric>
 __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V, const DevState S, int tile0,
                                                                 int max_local, float invdt2, float fb2)
 {
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
     }
     Block<float> acc;
     block_zero(acc);
-    tile_vertex_accumulate<G>(cx, tv.hv, tv.roff, lane, acc);
+    tile_vertex_accumulate<G, kGeneric>(cx, tv.hv, tv.roff, lane, acc, tv.ngen, V.gen_prm);
     group_reduce<G>(acc);
     allow_next_grid();
     if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tv.tg, invdt2, fb2);
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
 constexpr int kFlowMaxPolls = 1 << 21;  // with 128 ns sleeps and an L2 round trip: about a second per wait
 constexpr int kFlowPollMax = 64;       // neighbour-list entries prefetched per task (the rest are read directly)
 
-template <int G>
+template <int G, bool kGeneric>
 __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V, const DevState S,
                                                                 const FlowView F, int n_tiles, int iterations,
                                                                 int epoch_base, int max_local, float invdt2,
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     // polled: its record block and the indices of its local vertices (both into shared memory,
     // async), and the header, record offset and inertial target of the thread's vertex. The
     // target y is fixed for the whole step. The tile header comes from the prefetch.
-    auto fetch_static = [&](int4 &h0, int4 &h1, int4 &hv, int &roff, float4 &tg) {
+    auto fetch_static = [&](int4 &h0, int4 &h1, int4 &hv, int &roff, int &ngen, float4 &tg) {
         h0 = s_hdr[0];
         h1 = s_hdr[1];
         const int nvt = h0.y, nl = h0.y + h0.w;
@@ -215,10 +215,12 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         }
         hv = make_int4(0, 0, 0, 0);
         roff = 0;
+        ngen = 0;
         tg = make_float4(0.f, 0.f, 0.f, 0.f);
         if (lv < nvt) {
             hv = __ldg(S.hdr + h0.x + lv);
             roff = __ldg(V.vrec + h0.x + lv);
+            if (kGeneric) ngen = tile_generic_count(V, h0.x + lv);
             tg = S.tgt[h0.x + lv];
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -232,9 +234,9 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     __syncthreads();
     prefetch_poll(task);
     int4 h0, h1, hv;
-    int roff;
+    int roff, ngen;
     float4 tg;
-    if (task < total) fetch_static(h0, h1, hv, roff, tg);
+    if (task < total) fetch_static(h0, h1, hv, roff, ngen, tg);
     while (task < total) {
         const int k = task / n_tiles;
         const int tile = task - k * n_tiles;
@@ -294,7 +296,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         }
         Block<float> acc;
         block_zero(acc);
-        tile_vertex_accumulate<G>(cx, hv, roff, lane, acc);
+        tile_vertex_accumulate<G, kGeneric>(cx, hv, roff, lane, acc, ngen, V.gen_prm);
         group_reduce<G>(acc);
         if (active && lane == 0) solve_and_update(S, h0.x + lv, acc, sd[lv], tg, invdt2, fb2);
         __syncthreads();  // every position of the tile is written and the staging consumed
@@ -302,7 +304,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         // are visible to any CTA that acquires this epoch.
         if (threadIdx.x == 0) st_release_gpu(F.epoch + tile, epoch_base + k + 1);
         task = s_next;
-        if (task < total) fetch_static(h0, h1, hv, roff, tg);
+        if (task < total) fetch_static(h0, h1, hv, roff, ngen, tg);
     }
 }
 
@@ -322,7 +324,7 @@ __device__ __forceinline__ void block_sum_atomic(double v, double *out)
 }
 
 // Residual with the tile layout: every tile of every colour (positions are not modified).
-template <int G>
+template <int G, bool kGeneric>
 __global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileView V, const DevState S,
                                                                      int max_local, float invdt2, double *out)
 {
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(kTileThreads) residual_tile_kernel(const TileV
     }
     Block<float> acc;
     block_zero(acc);
-    tile_vertex_accumulate<G>(cx, tv.hv, tv.roff, lane, acc);
+    tile_vertex_accumulate<G, kGeneric>(cx, tv.hv, tv.roff, lane, acc, tv.ngen, V.gen_prm);
     group_reduce<G>(acc);
     double r2 = 0.0;
     if (active && lane == 0) {
@@ -448,6 +450,40 @@ static void launch_residual_lanes(int lanes, int grid, int block, cudaStream_t s
     }
 }
 
+template <bool kGen>
+static void launch_tile(const VbdSolver &s, int t0, int t1, int threads, cudaStream_t st, float invdt2, float fb2)
+{
+    switch (s.lanes) {
+    case 1: launch_pdl(vbd_tile_kernel<1, kGen>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+    case 2: launch_pdl(vbd_tile_kernel<2, kGen>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+    case 4: launch_pdl(vbd_tile_kernel<4, kGen>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+    default: launch_pdl(vbd_tile_kernel<8, kGen>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
+    }
+}
+
+template <bool kGen>
+static cudaError_t launch_flow_kernel(const VbdSolver &s, const cudaLaunchConfig_t &cfg, int n_tiles, int n, int base,
+                                      float invdt2, float fb2)
+{
+    switch (s.lanes) {
+    case 1: return cudaLaunchKernelEx(&cfg, vbd_flow_kernel<1, kGen>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2);
+    case 2: return cudaLaunchKernelEx(&cfg, vbd_flow_kernel<2, kGen>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2);
+    case 4: return cudaLaunchKernelEx(&cfg, vbd_flow_kernel<4, kGen>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2);
+    default: return cudaLaunchKernelEx(&cfg, vbd_flow_kernel<8, kGen>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2);
+    }
+}
+
+template <bool kGen>
+static void launch_residual_tile(const VbdSolver &s, int nt, int threads, cudaStream_t st, float invdt2, double *out)
+{
+    switch (s.lanes) {
+    case 1: residual_tile_kernel<1, kGen><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+    case 2: residual_tile_kernel<2, kGen><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+    case 4: residual_tile_kernel<4, kGen><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+    default: residual_tile_kernel<8, kGen><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
+    }
+}
+
 static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
 {
     if (s.kernel == 2) {
@@ -456,12 +492,10 @@ static void launch_color(const VbdSolver &s, int c, cudaStream_t st)
         const float invdt2 = static_cast<float>(1.0 / (s.h_sub * s.h_sub));
         const float fb2 = static_cast<float>(s.P.fallback_condition * s.P.fallback_condition);
         const int threads = s.TL.tile_vertices * s.lanes;
-        switch (s.lanes) {
-        case 1: launch_pdl(vbd_tile_kernel<1>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        case 2: launch_pdl(vbd_tile_kernel<2>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        case 4: launch_pdl(vbd_tile_kernel<4>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        default: launch_pdl(vbd_tile_kernel<8>, t1 - t0, threads, s.tile_smem, st, s.TV, s.S, t0, s.TL.max_local, invdt2, fb2); break;
-        }
+        if (s.TV.gen_off)
+            launch_tile<true>(s, t0, t1, threads, st, invdt2, fb2);
+        else
+            launch_tile<false>(s, t0, t1, threads, st, invdt2, fb2);
         return;
     }
     const int cs = s.L.color_start[c], ce = s.L.color_start[c + 1];
@@ -503,12 +537,8 @@ static void launch_flow(const VbdSolver &s, int n, cudaStream_t st)
     const int base = s.flow_epoch;
     cudaError_t e = cudaErrorInvalidConfiguration;  // warp 0 polls with full-warp votes: >= 32 threads
     if (cfg.blockDim.x >= 32) {
-        switch (s.lanes) {
-        case 1: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<1>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
-        case 2: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<2>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
-        case 4: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<4>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
-        default: e = cudaLaunchKernelEx(&cfg, vbd_flow_kernel<8>, s.TV, s.S, s.FV, n_tiles, n, base, s.TL.max_local, invdt2, fb2); break;
-        }
+        e = s.TV.gen_off ? launch_flow_kernel<true>(s, cfg, n_tiles, n, base, invdt2, fb2)
+                         : launch_flow_kernel<false>(s, cfg, n_tiles, n, base, invdt2, fb2);
     }
     // The counters only advance when the sweeps were enqueued; a failed launch is reported by
     // the caller's error check.
@@ -546,12 +576,10 @@ static void launch_residual(const VbdSolver &s, cudaStream_t st, double *out = n
         const int nt = s.TL.color_tiles.back();
         const int threads = s.TL.tile_vertices * s.lanes;
         if (nt > 0) {
-            switch (s.lanes) {
-            case 1: residual_tile_kernel<1><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
-            case 2: residual_tile_kernel<2><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
-            case 4: residual_tile_kernel<4><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
-            default: residual_tile_kernel<8><<<nt, threads, s.tile_smem, st>>>(s.TV, s.S, s.TL.max_local, invdt2, out); break;
-            }
+            if (s.TV.gen_off)
+                launch_residual_tile<true>(s, nt, threads, st, invdt2, out);
+            else
+                launch_residual_tile<false>(s, nt, threads, st, invdt2, out);
         }
         return;
     }
@@ -685,6 +713,8 @@ spgx_status VbdSolver::setup_tiles(int tv)
     TV.halo = tb_halo.as<int>();
     TV.records = tb_records.as<int4>();
     TV.vrec = tb_vrec.as<int>();
+    TV.gen_off = T.gen_off;
+    TV.gen_prm = T.gen_prm;
     TV.max_records = std::max(1, TL.max_records);
     tile_smem = tile_smem_bytes(std::max(1, TL.max_local), std::max(1, TL.max_records));
     // The opt-in limit is declared once for every tile kernel, whatever this scene needs: the
@@ -707,18 +737,20 @@ spgx_status VbdSolver::setup_tiles(int tv)
             return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         optin - static_cast<int>(a.sharedSizeBytes));
         };
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<1>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<2>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<4>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_tile_kernel<8>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<1>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<2>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<4>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(vbd_flow_kernel<8>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<1>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<2>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<4>)));
-        SPGX_CUDA(raise(reinterpret_cast<const void *>(residual_tile_kernel<8>)));
+        const void *fns[] = {
+            reinterpret_cast<const void *>(vbd_tile_kernel<1, false>), reinterpret_cast<const void *>(vbd_tile_kernel<2, false>),
+            reinterpret_cast<const void *>(vbd_tile_kernel<4, false>), reinterpret_cast<const void *>(vbd_tile_kernel<8, false>),
+            reinterpret_cast<const void *>(vbd_flow_kernel<1, false>), reinterpret_cast<const void *>(vbd_flow_kernel<2, false>),
+            reinterpret_cast<const void *>(vbd_flow_kernel<4, false>), reinterpret_cast<const void *>(vbd_flow_kernel<8, false>),
+            reinterpret_cast<const void *>(residual_tile_kernel<1, false>), reinterpret_cast<const void *>(residual_tile_kernel<2, false>),
+            reinterpret_cast<const void *>(residual_tile_kernel<4, false>), reinterpret_cast<const void *>(residual_tile_kernel<8, false>),
+            reinterpret_cast<const void *>(vbd_tile_kernel<1, true>), reinterpret_cast<const void *>(vbd_tile_kernel<2, true>),
+            reinterpret_cast<const void *>(vbd_tile_kernel<4, true>), reinterpret_cast<const void *>(vbd_tile_kernel<8, true>),
+            reinterpret_cast<const void *>(vbd_flow_kernel<1, true>), reinterpret_cast<const void *>(vbd_flow_kernel<2, true>),
+            reinterpret_cast<const void *>(vbd_flow_kernel<4, true>), reinterpret_cast<const void *>(vbd_flow_kernel<8, true>),
+            reinterpret_cast<const void *>(residual_tile_kernel<1, true>), reinterpret_cast<const void *>(residual_tile_kernel<2, true>),
+            reinterpret_cast<const void *>(residual_tile_kernel<4, true>), reinterpret_cast<const void *>(residual_tile_kernel<8, true>)};
+        for (const void *fn : fns) SPGX_CUDA(raise(fn));
     }
     return SPGX_OK;
 }
@@ -759,10 +791,15 @@ spgx_status VbdSolver::setup_flow()
     FV = FlowView{fl_fhdr.as<int2>(), fl_nbrp.as<int>(), fl_epoch.as<int>(), fl_ticket.as<int>()};
     SPGX_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
     const int T = TL.tile_vertices;
-    const void *fns[4] = {reinterpret_cast<const void *>(vbd_flow_kernel<1>),
-                          reinterpret_cast<const void *>(vbd_flow_kernel<2>),
-                          reinterpret_cast<const void *>(vbd_flow_kernel<4>),
-                          reinterpret_cast<const void *>(vbd_flow_kernel<8>)};
+    const bool gen = TV.gen_off != nullptr;
+    const void *fns[4] = {gen ? reinterpret_cast<const void *>(vbd_flow_kernel<1, true>)
+                              : reinterpret_cast<const void *>(vbd_flow_kernel<1, false>),
+                          gen ? reinterpret_cast<const void *>(vbd_flow_kernel<2, true>)
+                              : reinterpret_cast<const void *>(vbd_flow_kernel<2, false>),
+                          gen ? reinterpret_cast<const void *>(vbd_flow_kernel<4, true>)
+                              : reinterpret_cast<const void *>(vbd_flow_kernel<4, false>),
+                          gen ? reinterpret_cast<const void *>(vbd_flow_kernel<8, true>)
+                              : reinterpret_cast<const void *>(vbd_flow_kernel<8, false>)};
     const int gs[4] = {1, 2, 4, 8};
     for (int i = 0; i < 4; ++i) {
         flow_blocks_per_sm[i] = 0;
@@ -846,15 +883,8 @@ spgx_status VbdSolver::configure_launch()
         int kernel, lanes, block, tile;
     };
     const bool want_lanes = P.kernel == 0 || P.kernel == 1;
-    // Energies of types 6-14 are evaluated by the lanes kernel only (they are not in the
-    // tile records).
-    const bool generic = !L.gen_off.empty();
-    if (generic && (P.kernel == 2 || P.kernel == 3)) {
-        set_error("energy types 6-14 run on the lanes-per-vertex kernel (kernel 1) only");
-        return SPGX_ERR_INVALID_ARG;
-    }
-    const bool want_tiles = !generic && (P.kernel == 0 || P.kernel == 2);
-    const bool want_flow = !generic && (P.kernel == 0 || P.kernel == 3);
+    const bool want_tiles = P.kernel == 0 || P.kernel == 2;
+    const bool want_flow = P.kernel == 0 || P.kernel == 3;
     std::vector<int> tile_sizes;
     if (P.tile_vertices)
         tile_sizes.push_back(P.tile_vertices);

@@ -26,6 +26,11 @@ struct TileView {
     const int4 *records;
     const int *vrec;      // per internal vertex: record offset inside its tile's block
     int max_records;      // 16-byte record units of the largest tile
+    // Energies of types 6-14 (null when the scene has none): per internal vertex the range of
+    // its generic incidences (their count is the vertex's number of generic records), and the
+    // FP32 parameter table the records point into.
+    const int *gen_off;
+    const float *gen_prm;
 };
 
 // Tables of the dataflow kernel (vbd_flow_kernel).
@@ -84,8 +89,15 @@ struct TileCtx {
 struct TileVertex {
     int4 hv;     // incidence header
     int roff;    // record offset inside the tile's block
+    int ngen;    // generic (type 6-14) records after the six classes
     float4 tg;   // inertial target (y - base, mass)
 };
+
+// Generic incidences of internal vertex v (0 when the scene has none).
+__device__ __forceinline__ int tile_generic_count(const TileView &V, int v)
+{
+    return V.gen_off ? __ldg(V.gen_off + v + 1) - __ldg(V.gen_off + v) : 0;
+}
 
 // Stages the tile into shared memory. The tile's records and halo indices never change, so
 // they are fetched before waiting for the previous colour; the positions after. The header
@@ -104,10 +116,12 @@ __device__ __forceinline__ int4 tile_stage(const TileView &V, const DevState &S,
     const int lv = threadIdx.x / G;
     tv.hv = make_int4(0, 0, 0, 0);
     tv.roff = 0;
+    tv.ngen = 0;
     tv.tg = make_float4(0.f, 0.f, 0.f, 0.f);
     if (lv < nvt) {
         tv.hv = __ldg(S.hdr + h0.x + lv);
         tv.roff = __ldg(V.vrec + h0.x + lv);
+        tv.ngen = tile_generic_count(V, h0.x + lv);
     }
     constexpr int kMaxHaloPerThread = 8;
     int gidx[kMaxHaloPerThread];
@@ -136,10 +150,12 @@ __device__ __forceinline__ int4 tile_stage(const TileView &V, const DevState &S,
     return h0;
 }
 
-// Accumulates every incidence of one vertex from its staged records (G lanes, lane-strided).
-template <int G>
+// Accumulates every incidence of one vertex from its staged records (G lanes, lane-strided);
+// with kGeneric also its ngen records of energy types 6-14 (parameters in gen_prm).
+template <int G, bool kGeneric = false>
 __device__ __forceinline__ void tile_vertex_accumulate(const TileCtx &cx, int4 h, int roff, int lane,
-                                                       Block<float> &acc)
+                                                       Block<float> &acc, int ngen = 0,
+                                                       const float *__restrict__ gen_prm = nullptr)
 {
     const V3f zero = mk(0.f, 0.f, 0.f);
     int off = roff;
@@ -253,6 +269,22 @@ __device__ __forceinline__ void tile_vertex_accumulate(const TileCtx &cx, int4 h
                                     __int_as_float(b.z), __int_as_float(b.w), __int_as_float(c.x),
                                     __int_as_float(c.y), __int_as_float(c.z), __int_as_float(c.w)};
                 snh_block(p, a.z, D, __int_as_float(d.x), __int_as_float(d.y), __int_as_float(d.z), acc);
+            }
+        }
+        off += 4 * n;
+    }
+    if (kGeneric) {  // {v0 | v1 << 16, v2 | v3 << 16, type | slot << 8 | size << 16, parameter offset}
+        const int rounds = warp_max((ngen + G - 1) / G);
+        for (int r = 0; r < rounds; ++r) {
+            const int i = r * G + lane;
+            if (i < ngen) {
+                const int4 q = cx.rec[off + i];
+                const int type = q.z & 0xff, slot = (q.z >> 8) & 0xff, S = (q.z >> 16) & 0xff;
+                const int lj[4] = {q.x & 0xffff, q.x >> 16, q.y & 0xffff, q.y >> 16};
+                V3f p[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) p[j] = (j >= S || j == slot) ? zero : cx.rel(lj[j]);
+                generic_block(type, p, slot, gen_prm + q.w, acc);
             }
         }
     }

@@ -144,13 +144,14 @@ def test_device_blocks_match_oracle():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 @pytest.mark.parametrize("name", ["stvk_tet_load", "ssnh", "bw", "choi_quad", "springs"])
-def test_positions_after_10_steps_match_oracle(name):
+def test_positions_after_10_steps_match_oracle(name, kernel):
     N = pytest.importorskip("spg_gb300.native")
     obj = _variant_scenes()[name]
     kw = dict(dt=1 / 60, iterations=30, gravity=scenes.GRAVITY)
-    gpu = N.VbdSolver([obj], **kw)
-    assert gpu.launch()[0] == 1  # these energies run on the lanes kernel
+    gpu = N.VbdSolver([obj], kernel=kernel, **kw)
+    assert gpu.launch()[0] == kernel
     ref = O.Vbd(obj, 1 / 60, 1, 30, scenes.GRAVITY, O.VERTEX_AD)
     for _ in range(10):
         gpu.step()
@@ -164,12 +165,25 @@ def test_positions_after_10_steps_match_oracle(name):
 
 
 @pytest.mark.gpu
-def test_tile_kernels_refuse_these_energies_and_xpbd_the_load():
+@pytest.mark.parametrize("name", ["stvk_tet_load", "bw", "choi_quad", "springs"])
+def test_tile_kernels_run_these_energies_bit_exactly(name):
+    """Energies 6-14 in the tile records (one 16-byte record per incidence, parameters in the
+    generic table): the per-colour tile launches and the dataflow kernel run the same sweeps,
+    bit for bit, with the same lanes and tile size."""
     N = pytest.importorskip("spg_gb300.native")
-    obj = _variant_scenes()["bw"]
-    for k in (2, 3):
-        with pytest.raises(N.SpgxError):
-            N.VbdSolver([obj], dt=1 / 60, iterations=5, gravity=scenes.GRAVITY, kernel=k)
+    obj = _variant_scenes()[name]
+    kw = dict(dt=1 / 60, iterations=20, gravity=scenes.GRAVITY, lanes_per_vertex=4, tile_vertices=32)
+    a = N.VbdSolver([obj], kernel=2, **kw)
+    b = N.VbdSolver([obj], kernel=3, **kw)
+    for _ in range(3):
+        a.step()
+        b.step()
+    assert np.array_equal(a.state(0)[0], b.state(0)[0])
+
+
+@pytest.mark.gpu
+def test_xpbd_refuses_the_static_load():
+    N = pytest.importorskip("spg_gb300.native")
     with pytest.raises(N.SpgxError, match="load"):
         N.XpbdSolver([scenes.spring_variant(load=True)], dt=1 / 60, substeps=2, gravity=scenes.GRAVITY)
 
