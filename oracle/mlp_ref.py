@@ -76,26 +76,31 @@ def forward(w, x, emulate_bf16_activations=False):
     return h @ q["W4"] + q["b4"]
 
 
-def loss_grad(w, x, t, quantize=True):
-    """FP64 mean-squared-error loss and its gradient with respect to the flat weights."""
+def loss_grad(w, x, t, quantize=True, emulate_bf16_operands=False):
+    """FP64 mean-squared-error loss and its gradient with respect to the flat weights. With
+    emulate_bf16_operands every operand of the eleven matrix products is rounded to BF16 first,
+    as the tensor-core GEMMs of the device training take them (the FP32 values are kept for
+    the bias, GELU and loss arithmetic)."""
     q = quantized(w, quantize)
     x = np.asarray(x, dtype=np.float64)
     t = np.asarray(t, dtype=np.float64)
-    z1 = x @ q["W1"] + q["b1"]
+    r = (lambda a: bf16_round(np.asarray(a, dtype=np.float32)).astype(np.float64)) if emulate_bf16_operands \
+        else (lambda a: a)
+    z1 = r(x) @ q["W1"] + q["b1"]
     a1 = gelu(z1)
-    z2 = a1 @ q["W2"] + q["b2"]
+    z2 = r(a1) @ q["W2"] + q["b2"]
     a2 = gelu(z2)
-    z3 = a2 @ q["W3"] + q["b3"]
+    z3 = r(a2) @ q["W3"] + q["b3"]
     a3 = gelu(z3)
-    y = a3 @ q["W4"] + q["b4"]
+    y = r(a3) @ q["W4"] + q["b4"]
     e = y - t
     loss = float(np.mean(e * e))
     dy = 2.0 * e / e.size
-    g = {"W4": a3.T @ dy, "b4": dy.sum(0)}
-    d3 = (dy @ q["W4"].T) * gelu_grad(z3)
-    g["W3"], g["b3"] = a2.T @ d3, d3.sum(0)
-    d2 = (d3 @ q["W3"].T) * gelu_grad(z2)
-    g["W2"], g["b2"] = a1.T @ d2, d2.sum(0)
-    d1 = (d2 @ q["W2"].T) * gelu_grad(z1)
-    g["W1"], g["b1"] = x.T @ d1, d1.sum(0)
+    g = {"W4": r(a3).T @ r(dy), "b4": dy.sum(0)}
+    d3 = (r(dy) @ q["W4"].T) * gelu_grad(z3)
+    g["W3"], g["b3"] = r(a2).T @ r(d3), d3.sum(0)
+    d2 = (r(d3) @ q["W3"].T) * gelu_grad(z2)
+    g["W2"], g["b2"] = r(a1).T @ r(d2), d2.sum(0)
+    d1 = (r(d2) @ q["W2"].T) * gelu_grad(z1)
+    g["W1"], g["b1"] = r(x).T @ r(d1), d1.sum(0)
     return loss, pack(g)

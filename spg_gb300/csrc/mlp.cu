@@ -6,9 +6,10 @@
 // per CTA at a time; each layer's accumulator is read back with tcgen05.ld, biased, passed
 // through GELU and rounded to BF16 as the next layer's operand.
 //
-// Training runs FP32 SIMT kernels (a tiled GEMM, GELU forward/backward, bias reductions, Adam)
-// on FP32 master weights whose BF16 rounding is used in the forward pass, so the trained
-// network is the one the BF16 inference kernel evaluates (straight-through for the rounding).
+// Training runs its eleven GEMMs on the tensor cores too (gemm_tc_kernel: BF16 operands, FP32
+// accumulation) and GELU forward/backward, bias reductions and Adam as SIMT kernels, on FP32
+// master weights whose BF16 rounding is used in the forward pass, so the trained network is
+// the one the BF16 inference kernel evaluates (straight-through for the rounding).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -357,51 +358,129 @@ __global__ void mlp_pack_kernel(const float *__restrict__ w, __nv_bfloat16 *w1t,
 // ---------------------------------------------------------------------------------------
 // Training (FP32 SIMT)
 
-// C[M x N] = alpha * op(A) * op(B) + beta * C, row-major, op = transpose when the flag is set.
-// 64 x 64 output tile per 256-thread block, 4 x 4 outputs per thread, K chunks of 16.
-__global__ void __launch_bounds__(256) gemm_f32_kernel(int M, int N, int K, const float *__restrict__ A, int lda,
-                                                       bool tA, const float *__restrict__ B, int ldb, bool tB, float *C,
-                                                       int ldc, float alpha, float beta)
+// C[M x N] = op(A) * op(B) + beta * C on the tensor cores, row-major FP32 arrays, op =
+// transpose when the flag is set. One CTA computes a 128 x NT tile (NT = 128, or 16 when
+// N <= 16) over K in chunks of 64: the threads stage op(A) (128 x 64) and op(B)^T (NT x 64)
+// as BF16 in the K-major core-matrix layout of the inference kernel (coalesced along
+// whichever dimension is contiguous in memory; zeros outside the matrices), one thread issues
+// the chunk's four tcgen05.mma (K = 16 each) into the FP32 accumulator in tensor memory and
+// commits them to an mbarrier, and after the last chunk each warp reads its 32 rows back with
+// tcgen05.ld. BF16 operands with FP32 accumulation, as the network's inference evaluates it.
+// Long K (the weight gradients, summed over the batch) is split over gridDim.z CTAs whose
+// partial tiles are added into C with atomics.
+namespace tcg {
+
+constexpr int kKC = 64;                          // K per chunk
+constexpr int kA = 0;                            // 128 x 64 BF16
+constexpr int kB = kA + 128 * kKC * 2;           // up to 128 x 64 BF16
+constexpr int kBar = kB + 128 * kKC * 2;
+constexpr int kSlot = kBar + 8;
+// Padded so that at most four CTAs share an SM: four 128-column accumulators fill its tensor
+// memory, so an allocation never waits on a CTA that is not resident.
+constexpr size_t kSmem = 56 * 1024;
+
+}  // namespace tcg
+
+__global__ void __launch_bounds__(128) gemm_tc_kernel(int M, int N, int K, const float *__restrict__ A, int lda,
+                                                      bool tA, const float *__restrict__ B, int ldb, bool tB,
+                                                      float *C, int ldc, float beta, int NT, unsigned int *status)
 {
-    __shared__ float As[16][64 + 1];
-    __shared__ float Bs[16][64 + 1];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        for (int i = threadIdx.x; i < 16 * 64; i += 256) {
-            const int kk = i / 64, mm = i % 64;
-            const int gm = m0 + mm, gk = k0 + kk;
-            As[kk][mm] = (gm < M && gk < K) ? (tA ? A[size_t(gk) * lda + gm] : A[size_t(gm) * lda + gk]) : 0.f;
-            const int gn = n0 + mm;
-            Bs[kk][mm] = (gn < N && gk < K) ? (tB ? B[size_t(gn) * ldb + gk] : B[size_t(gk) * ldb + gn]) : 0.f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < 16; ++kk) {
-            float av[4], bv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                av[q] = As[kk][ty * 4 + q];
-                bv[q] = Bs[kk][tx * 4 + q];
-            }
-#pragma unroll
-            for (int p = 0; p < 4; ++p)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) acc[p][q] += av[p] * bv[q];
-        }
-        __syncthreads();
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = smem_raw + ((1024 - (static_cast<uint32_t>(__cvta_generic_to_shared(smem_raw)) & 1023)) & 1023);
+    const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(sm));
+    const uint32_t bar = sbase + tcg::kBar;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + tcg::kSlot);
+    __nv_bfloat16 *sA = reinterpret_cast<__nv_bfloat16 *>(sm + tcg::kA);
+    __nv_bfloat16 *sB = reinterpret_cast<__nv_bfloat16 *>(sm + tcg::kB);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.y * 128, n0 = blockIdx.x * NT;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         static_cast<uint32_t>(__cvta_generic_to_shared(slot))),
+                     "r"(128)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int gm = m0 + ty * 4 + p, gn = n0 + tx * 4 + q;
-            if (gm < M && gn < N) {
-                float *c = C + size_t(gm) * ldc + gn;
-                *c = alpha * acc[p][q] + (beta == 0.f ? 0.f : beta * *c);
-            }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *slot;
+    // op(A)(m, k) and op(B)(k, n); the staging order follows the contiguous dimension.
+    auto a_at = [&](int m, int k) -> float {
+        return (m < M && k < K) ? (tA ? A[size_t(k) * lda + m] : A[size_t(m) * lda + k]) : 0.f;
+    };
+    auto b_at = [&](int k, int n) -> float {
+        return (n < N && k < K) ? (tB ? B[size_t(n) * ldb + k] : B[size_t(k) * ldb + n]) : 0.f;
+    };
+    uint32_t phase = 0;
+    bool ok = true;
+    // Split K (gridDim.z > 1, beta = 0, C zeroed by the caller): this CTA sums its share of the
+    // chunks and adds its partial tile into C.
+    const int all_chunks = (K + tcg::kKC - 1) / tcg::kKC;
+    const int per = (all_chunks + gridDim.z - 1) / gridDim.z;
+    const int c_begin = blockIdx.z * per, c_end = min(all_chunks, c_begin + per);
+    for (int c = c_begin; c < c_end && ok; ++c) {
+        const int k0 = c * tcg::kKC;
+#pragma unroll 16
+        for (int e = tid; e < 128 * tcg::kKC; e += blockDim.x) {
+            const int m = tA ? e % 128 : e / tcg::kKC, k = tA ? e / 128 : e % tcg::kKC;
+            sA[tc::core_off(m, k, tcg::kKC) / 2] = __float2bfloat16_rn(a_at(m0 + m, k0 + k));
         }
+#pragma unroll 16
+        for (int e = tid; e < NT * tcg::kKC; e += blockDim.x) {
+            const int n = tB ? e / tcg::kKC : e % NT, k = tB ? e % tcg::kKC : e / NT;
+            sB[tc::core_off(n, k, tcg::kKC) / 2] = __float2bfloat16_rn(b_at(k0 + k, n0 + n));
+        }
+        tc::fence_async_smem();
+        tc::fence_before();
+        __syncthreads();
+        tc::fence_after();
+        if (tid == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, NT);
+            for (int ks = 0; ks < tcg::kKC / 16; ++ks) {
+                const uint64_t a = tc::smem_desc(sbase + tcg::kA + ks * 256, 128, (tcg::kKC / 8) * 128);
+                const uint64_t bdesc = tc::smem_desc(sbase + tcg::kB + ks * 256, 128, (tcg::kKC / 8) * 128);
+                tc::mma(tmem, a, bdesc, idesc, (c > c_begin || ks > 0) ? 1u : 0u);
+            }
+            tc::commit(bar);
+        }
+        // The chunk's operands are read before the next chunk overwrites them.
+        ok = __syncthreads_and(tc::wait_phase(bar, phase));
+        phase ^= 1u;
+        tc::fence_after();
+    }
+    if (ok && c_end > c_begin) {
+        const int m = m0 + tid;
+        const uint32_t lane_base = uint32_t(warp * 32) << 16;
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+            float v[16];
+            tc::ld16(tmem + lane_base + uint32_t(c0), v);
+            if (m < M)
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = n0 + c0 + j;
+                    if (n < N) {
+                        float *cp = C + size_t(m) * ldc + n;
+                        if (gridDim.z > 1)
+                            atomicAdd(cp, v[j]);
+                        else
+                            *cp = v[j] + (beta == 0.f ? 0.f : beta * *cp);
+                    }
+                }
+        }
+    } else {
+        if (tid == 0) atomicOr(status, 1u);
+        tc::wait_phase(bar, phase ^ 1u);
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128) : "memory");
 }
 
 // Z += bias (per column); A = gelu(Z) when act.
@@ -486,10 +565,15 @@ __global__ void gather_rows_kernel(const float *X, const int *idx, float *Xb, in
 static int blocks_for(size_t n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
 
 static void gemm(cudaStream_t st, int M, int N, int K, const float *A, int lda, bool tA, const float *B, int ldb,
-                 bool tB, float *C, int ldc, float beta)
+                 bool tB, float *C, int ldc, float beta, unsigned int *status)
 {
-    dim3 grid((N + 63) / 64, (M + 63) / 64);
-    gemm_f32_kernel<<<grid, 256, 0, st>>>(M, N, K, A, lda, tA, B, ldb, tB, C, ldc, 1.f, beta);
+    const int NT = N <= 16 ? 16 : 128;
+    // The weight gradients sum over the whole batch (K = rows): their K is split over CTAs.
+    int splits = 1;
+    if (beta == 0.f && ldc == N && K > 1024) splits = std::min(64, (K + 127) / 128);
+    if (splits > 1) cudaMemsetAsync(C, 0, size_t(M) * N * sizeof(float), st);
+    dim3 grid((N + NT - 1) / NT, (M + 127) / 128, splits);
+    gemm_tc_kernel<<<grid, 128, tcg::kSmem, st>>>(M, N, K, A, lda, tA, B, ldb, tB, C, ldc, beta, NT, status);
 }
 
 spgx_status Mlp::init(uint64_t seed, int dev)
@@ -510,6 +594,8 @@ spgx_status Mlp::init(uint64_t seed, int dev)
     SPGX_TRY_STATUS(d_loss.alloc(sizeof(double)));
     SPGX_CUDA(cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(tc::kSmem)));
+    SPGX_CUDA(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(tcg::kSmem)));
     SPGX_TRY_STATUS(d_status.alloc(sizeof(unsigned int)));
     SPGX_CUDA(cudaMemset(d_status.as<void>(), 0, sizeof(unsigned int)));
     SPGX_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
@@ -603,32 +689,32 @@ spgx_status Mlp::loss_grad_device(const float *X, const float *T, int M, double 
     float *g = d_g.as<float>();
     const int H = kMlpHidden;
     // forward
-    gemm(stream, M, H, kMlpIn, X, kMlpIn, false, wq + kMlpOffW1, H, false, z1.as<float>(), H, 0.f);
+    gemm(stream, M, H, kMlpIn, X, kMlpIn, false, wq + kMlpOffW1, H, false, z1.as<float>(), H, 0.f, d_status.as<unsigned int>());
     bias_act_kernel<<<blocks_for(size_t(M) * H), 256, 0, stream>>>(z1.as<float>(), a1.as<float>(), wq + kMlpOffB1, M, H, true);
-    gemm(stream, M, H, H, a1.as<float>(), H, false, wq + kMlpOffW2, H, false, z2.as<float>(), H, 0.f);
+    gemm(stream, M, H, H, a1.as<float>(), H, false, wq + kMlpOffW2, H, false, z2.as<float>(), H, 0.f, d_status.as<unsigned int>());
     bias_act_kernel<<<blocks_for(size_t(M) * H), 256, 0, stream>>>(z2.as<float>(), a2.as<float>(), wq + kMlpOffB2, M, H, true);
-    gemm(stream, M, H, H, a2.as<float>(), H, false, wq + kMlpOffW3, H, false, z3.as<float>(), H, 0.f);
+    gemm(stream, M, H, H, a2.as<float>(), H, false, wq + kMlpOffW3, H, false, z3.as<float>(), H, 0.f, d_status.as<unsigned int>());
     bias_act_kernel<<<blocks_for(size_t(M) * H), 256, 0, stream>>>(z3.as<float>(), a3.as<float>(), wq + kMlpOffB3, M, H, true);
-    gemm(stream, M, 3, H, a3.as<float>(), H, false, wq + kMlpOffW4, 3, false, yb.as<float>(), 3, 0.f);
+    gemm(stream, M, 3, H, a3.as<float>(), H, false, wq + kMlpOffW4, 3, false, yb.as<float>(), 3, 0.f, d_status.as<unsigned int>());
     bias_act_kernel<<<blocks_for(size_t(M) * 3), 256, 0, stream>>>(yb.as<float>(), nullptr, wq + kMlpOffB4, M, 3, false);
     // loss
     SPGX_CUDA(cudaMemsetAsync(d_loss.as<double>(), 0, sizeof(double), stream));
     mse_grad_kernel<<<blocks_for(size_t(M) * 3), 256, 0, stream>>>(yb.as<float>(), T, dy.as<float>(), M,
                                                                     d_loss.as<double>());
     // backward
-    gemm(stream, H, 3, M, a3.as<float>(), H, true, dy.as<float>(), 3, false, g + kMlpOffW4, 3, 0.f);
+    gemm(stream, H, 3, M, a3.as<float>(), H, true, dy.as<float>(), 3, false, g + kMlpOffW4, 3, 0.f, d_status.as<unsigned int>());
     col_sum_kernel<<<3, 256, 0, stream>>>(dy.as<float>(), g + kMlpOffB4, M, 3);
-    gemm(stream, M, H, 3, dy.as<float>(), 3, false, wq + kMlpOffW4, 3, true, da.as<float>(), H, 0.f);
+    gemm(stream, M, H, 3, dy.as<float>(), 3, false, wq + kMlpOffW4, 3, true, da.as<float>(), H, 0.f, d_status.as<unsigned int>());
     gelu_back_kernel<<<blocks_for(size_t(M) * H), 256, 0, stream>>>(da.as<float>(), z3.as<float>(), size_t(M) * H);
-    gemm(stream, H, H, M, a2.as<float>(), H, true, da.as<float>(), H, false, g + kMlpOffW3, H, 0.f);
+    gemm(stream, H, H, M, a2.as<float>(), H, true, da.as<float>(), H, false, g + kMlpOffW3, H, 0.f, d_status.as<unsigned int>());
     col_sum_kernel<<<H, 256, 0, stream>>>(da.as<float>(), g + kMlpOffB3, M, H);
-    gemm(stream, M, H, H, da.as<float>(), H, false, wq + kMlpOffW3, H, true, db_.as<float>(), H, 0.f);
+    gemm(stream, M, H, H, da.as<float>(), H, false, wq + kMlpOffW3, H, true, db_.as<float>(), H, 0.f, d_status.as<unsigned int>());
     gelu_back_kernel<<<blocks_for(size_t(M) * H), 256, 0, stream>>>(db_.as<float>(), z2.as<float>(), size_t(M) * H);
-    gemm(stream, H, H, M, a1.as<float>(), H, true, db_.as<float>(), H, false, g + kMlpOffW2, H, 0.f);
+    gemm(stream, H, H, M, a1.as<float>(), H, true, db_.as<float>(), H, false, g + kMlpOffW2, H, 0.f, d_status.as<unsigned int>());
     col_sum_kernel<<<H, 256, 0, stream>>>(db_.as<float>(), g + kMlpOffB2, M, H);
-    gemm(stream, M, H, H, db_.as<float>(), H, false, wq + kMlpOffW2, H, true, da.as<float>(), H, 0.f);
+    gemm(stream, M, H, H, db_.as<float>(), H, false, wq + kMlpOffW2, H, true, da.as<float>(), H, 0.f, d_status.as<unsigned int>());
     gelu_back_kernel<<<blocks_for(size_t(M) * H), 256, 0, stream>>>(da.as<float>(), z1.as<float>(), size_t(M) * H);
-    gemm(stream, kMlpIn, H, M, X, kMlpIn, true, da.as<float>(), H, false, g + kMlpOffW1, H, 0.f);
+    gemm(stream, kMlpIn, H, M, X, kMlpIn, true, da.as<float>(), H, false, g + kMlpOffW1, H, 0.f, d_status.as<unsigned int>());
     col_sum_kernel<<<H, 256, 0, stream>>>(da.as<float>(), g + kMlpOffB1, M, H);
     SPGX_CUDA(cudaGetLastError());
     if (loss_out) {
@@ -791,7 +877,7 @@ spgx_status spgx_mlp_loss_grad(spgx_mlp *h, int32_t n, const float *x, const flo
                               h->m->stream));
     SPGX_CUDA(cudaStreamSynchronize(h->m->stream));
     *loss = static_cast<float>(l);
-    return SPGX_OK;
+    return h->m->take_status();
     SPGX_GUARD_END
 }
 
@@ -804,7 +890,9 @@ spgx_status spgx_mlp_train(spgx_mlp *h, int32_t n, const float *x, const float *
         spgx::set_error("invalid argument");
         return SPGX_ERR_INVALID_ARG;
     }
-    return h->m->train(x, y, n, steps, batch, lr, seed, final_loss);
+    SPGX_TRY_STATUS(h->m->train(x, y, n, steps, batch, lr, seed, final_loss));
+    SPGX_CUDA(cudaStreamSynchronize(h->m->stream));
+    return h->m->take_status();
     SPGX_GUARD_END
 }
 

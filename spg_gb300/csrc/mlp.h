@@ -30,7 +30,7 @@ struct Mlp {
     DevBuf d_w, d_wq, d_g, d_m, d_v;         // master weights, BF16-rounded copy, grad, Adam moments
     DevBuf d_w1t, d_w2t, d_w3t, d_w4t, d_b4;  // BF16 transposed copies for inference
     DevBuf d_loss;
-    DevBuf d_status;  // bit 0: an inference tile's tensor-core commit never arrived (bounded wait)
+    DevBuf d_status;  // bit 0: a tensor-core commit (inference or training GEMM) never arrived (bounded wait)
     int num_sms{0};
     DevBuf z1, a1, z2, a2, z3, a3, yb, dy, da, db_, xb, tb, ib;
     int batch_cap{0};

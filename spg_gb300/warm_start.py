@@ -198,11 +198,14 @@ def main(argv=None):
     ap.add_argument("--max-iterations", type=int, default=3000)
     ap.add_argument("--time-budget", type=float, default=600.0, help="seconds of data generation at most")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--sizes", type=int, nargs="+", default=[65, 129],
+                    help="patch side lengths (vertices), one per episode in turn")
     args = ap.parse_args(argv)
     os.makedirs(args.out, exist_ok=True)
     t0 = time.time()
     X, Y = generate(episodes=args.episodes, steps=args.steps, keep=args.keep, tol=args.tol,
-                    max_iterations=args.max_iterations, device=args.device, time_budget=args.time_budget)
+                    max_iterations=args.max_iterations, device=args.device, time_budget=args.time_budget,
+                    sizes=tuple(args.sizes))
     t_gen = time.time() - t0
     print(f"{X.shape[0]} rows in {t_gen:.0f} s; target rms {np.sqrt(np.mean(Y ** 2)):.4g}", flush=True)
     # Held-out rows (the last 2 %) measure the fit.
@@ -214,7 +217,8 @@ def main(argv=None):
     base = float(np.mean(Y[cut:] ** 2))
     w = mlp.weights()
     np.save(os.path.join(args.out, "warm_start_spring_cloth.npy"), w)
-    meta = {"rows": int(m), "episodes": args.episodes, "steps_per_episode": args.steps, "row_fraction": args.keep,
+    meta = {"rows": int(m), "episodes": args.episodes, "sizes": list(args.sizes), "steps_per_episode": args.steps,
+            "row_fraction": args.keep,
             "tolerance": args.tol, "max_iterations": args.max_iterations, "generation_s": t_gen, "stages": hist,
             "output_scale": scale, "heldout_mse": mse, "heldout_mse_of_zero_guess": base,
             "params": int(w.size)}

@@ -66,8 +66,11 @@ def test_num_params_matches_oracle():
 
 @pytest.mark.gpu
 def test_loss_gradient_matches_oracle():
-    """FP32 forward/backward on the device against the FP64 oracle (same BF16-rounded weights):
-    gradient within 1e-4 of its largest entry, per weight block."""
+    """Device forward/backward (tensor-core GEMMs with BF16 operands, FP32 accumulation) against
+    the FP64 oracle with the same BF16 roundings of the weights and of every GEMM operand:
+    gradient within 2e-3 of its largest entry per weight block (FP32 accumulation order, and an
+    operand whose FP32 value sits next to a BF16 rounding boundary rounding the other way), and
+    within 3e-2 of the unrounded FP64 gradient."""
     rng = np.random.default_rng(2)
     mlp = N.Mlp(seed=3)
     w = _weights(rng)
@@ -76,13 +79,18 @@ def test_loss_gradient_matches_oracle():
     x = _features(rng, 3000)
     t = rng.normal(size=(3000, 3)).astype(np.float32)
     loss, g = mlp.loss_grad(x, t)
-    loss_ref, g_ref = M.loss_grad(w, x, t)
-    assert abs(loss - loss_ref) <= 1e-5 * loss_ref
+    loss_ref, g_ref = M.loss_grad(w, x, t, emulate_bf16_operands=True)
+    _, g_full = M.loss_grad(w, x, t)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
     o = 0
     for name, shape in M.SHAPES:
         n = int(np.prod(shape))
-        a, b = g[o:o + n], g_ref[o:o + n]
-        assert np.max(np.abs(a - b)) <= 1e-4 * np.max(np.abs(b)), name
+        a, b, c = g[o:o + n], g_ref[o:o + n], g_full[o:o + n]
+        err = np.max(np.abs(a - b)) / np.max(np.abs(b))
+        print(f"{name}: max |g - g_bf16| / max |g_bf16| = {err:.2e}, against unrounded "
+              f"{np.max(np.abs(a - c)) / np.max(np.abs(c)):.2e}")
+        assert err <= 2e-3, name
+        assert np.max(np.abs(a - c)) <= 3e-2 * np.max(np.abs(c)), name
         o += n
 
 
