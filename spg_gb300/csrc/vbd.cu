@@ -174,6 +174,10 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
     __shared__ int2 s_fh;
     __shared__ int s_poll[kFlowPollMax];
     __shared__ int s_next, s_fail;
+    // Completion of the record block's bulk copy (one phase per task).
+    __shared__ __align__(8) unsigned long long s_rec_bar;
+    const uint32_t rec_bar = static_cast<uint32_t>(__cvta_generic_to_shared(&s_rec_bar));
+    uint32_t rec_phase = 0;
     const int total = iterations * n_tiles;
     const int lv = threadIdx.x / G;
     const int lane = threadIdx.x & (G - 1);
@@ -206,7 +210,21 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         h0 = s_hdr[0];
         h1 = s_hdr[1];
         const int nvt = h0.y, nl = h0.y + h0.w;
-        for (int i = threadIdx.x; i < h1.y; i += blockDim.x) cp_async16(srec + i, V.records + h1.x + i);
+        // The record block (contiguous, 16-byte aligned, a multiple of 16 bytes) in one bulk copy
+        // by the tensor memory accelerator, completed on s_rec_bar: one instruction instead of a
+        // 16-byte copy per record. The block's previous contents were last read before the
+        // barrier that preceded this call; the proxy fence orders those reads before the copy.
+        if (threadIdx.x == 0 && h1.y > 0) {
+            const uint32_t bytes = static_cast<uint32_t>(h1.y) * 16u;
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(rec_bar), "r"(bytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                    static_cast<uint32_t>(__cvta_generic_to_shared(srec))),
+                "l"(V.records + h1.x), "r"(bytes), "r"(rec_bar)
+                : "memory");
+        }
         for (int i = threadIdx.x; i < nl; i += blockDim.x) {
             if (i < nvt)
                 sidx[i] = h0.x + i;
@@ -226,9 +244,30 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
 
-    if (threadIdx.x == 0) s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
+    if (threadIdx.x == 0) {
+        s_next = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(rec_bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
     __syncthreads();
     int task = s_next;
+    // Bounded wait for the record block of the task fetched last (its bulk copy has arrived
+    // once the mbarrier phase completes); false when the polls ran out.
+    auto wait_records = [&](int n_rec) -> bool {
+        if (n_rec <= 0) return true;
+        for (int i = 0; i < kFlowMaxPolls; ++i) {
+            uint32_t done;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}\n"
+                : "=r"(done)
+                : "r"(rec_bar), "r"(rec_phase)
+                : "memory");
+            if (done) return true;
+            __nanosleep(32);
+        }
+        return false;
+    };
     prefetch_header(task);
     cp_async_wait_all();
     __syncthreads();
@@ -275,6 +314,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
                 atomicExch(F.ticket + 1, 1);
                 atomicOr(S.status, 2u);
             }
+            wait_records(h1.y);  // the record copy in flight lands before the CTA leaves
             break;
         }
         prefetch_header(s_next);
@@ -287,7 +327,15 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
         }
         const bool active = lv < h0.y;
         cp_async_wait_all();
-        __syncthreads();  // the staging and the next task's header
+        const bool rec_ok = wait_records(h1.y);
+        if (h1.y > 0) rec_phase ^= 1u;
+        if (!__syncthreads_and(rec_ok)) {  // the staging, the records and the next task's header
+            if (threadIdx.x == 0) {
+                atomicExch(F.ticket + 1, 1);
+                atomicOr(S.status, 2u);
+            }
+            break;
+        }
         prefetch_poll(s_next);
         TileCtx cx{sb, sd, srec, mk(0.f, 0.f, 0.f), mk(0.f, 0.f, 0.f)};
         if (active) {
