@@ -425,6 +425,10 @@ typedef struct spgx_implicit_params {
     int32_t cg_max_iterations; /* ImplicitEulerBase::m_cgMaxIterations (300) */
     int32_t device;
     int32_t method;            /* an spgx_implicit_method value; default NEWTON_DX */
+    int32_t cg_precision;      /* 0 (default): the CG runs in double-float (FP32 hi/lo pairs, 48
+                                * significant bits) on a symmetric matrix, as one launch per solve,
+                                * and in FP64 when the system leaves that range (above 2^60);
+                                * 1: always FP64 (one launch per kernel). */
 } spgx_implicit_params;
 
 void spgx_implicit_params_default(spgx_implicit_params *p);

@@ -58,16 +58,14 @@ struct ImplicitTables {
     const int *col;      // BSR block columns
     double *val;         // BSR values, 9 per block (row-major)
     const int *diag;     // per vertex: position of its diagonal block
-    float2 *val2;        // the CG's system matrix in double-float form (split_df), entry-major:
-                         // entry q (row-major in the block) of block k at val2[q * nnzb + k]
-    int *wide;           // set when the CG's matrix or direction leaves the double-float range
+    int *wide;           // set when the CG's matrix leaves the double-float range
     int nnzb;            // number of blocks
 };
 
 // Double-float form of an FP64 value: a = hi + lo with hi = fl32(a) and lo = fl32(a - hi),
-// 48 significant bits. GB300 runs FP64 at about 1/64 of its FP32 rate, so the CG's products
-// (the solve's only O(nnz) arithmetic) run on the FP32 pipes in this form. A value above 2^60
-// in magnitude, or not finite, reports out of range: the SpMV then falls back to FP64.
+// 48 significant bits. GB300 runs FP64 at about 1/64 of its FP32 rate, so the CG runs on the
+// FP32 pipes in this form. A value above 2^60 in magnitude, or not finite, reports out of
+// range: the solve then runs in FP64.
 __device__ __forceinline__ float2 split_df(double a, bool &out_of_range)
 {
     out_of_range = !(fabs(a) <= 0x1p60);
@@ -397,18 +395,18 @@ __global__ void implicit_lhs_kernel(ImplicitTables T, const double *mass, int nv
     dinv[3 * i + 2] = b[8] != 0.0 ? 1.0 / b[8] : 1.0;
 }
 
-// val2 = split_df(val) over all 9 nnzb values, transposed to the entry-major layout (the
-// SpMV's lanes then read consecutive blocks with coalesced 8-byte loads). A nonzero
-// diagonal below 2^-60 in magnitude (a row whose scale nears FP32's underflow) also selects
-// the FP64 SpMV.
-__global__ void implicit_split_kernel(ImplicitTables T, size_t n_values, int nv)
+// The CG's symmetric double-float matrix: the 9 entries of every upper block (ufull: its
+// position in the full pattern) as split_df pairs, one 80-byte record per block (10 pairs, the
+// last zero). A nonzero diagonal below 2^-60 in magnitude (a row whose scale nears FP32's
+// underflow) also selects the FP64 solve.
+__global__ void implicit_split_kernel(ImplicitTables T, float2 *ublk, const int *ufull, int nnzu, int nv)
 {
     bool bad = false;
-    const size_t nb = size_t(T.nnzb);
+    const size_t n_values = 10 * size_t(nnzu);
     for (size_t o = blockIdx.x * size_t(blockDim.x) + threadIdx.x; o < n_values; o += size_t(gridDim.x) * blockDim.x) {
-        const size_t q = o / nb, k = o - q * nb;
-        bool out;
-        T.val2[o] = split_df(T.val[k * 9 + q], out);
+        const size_t k = o / 10, q = o - k * 10;
+        bool out = false;
+        ublk[o] = q < 9 ? split_df(T.val[size_t(__ldg(ufull + k)) * 9 + q], out) : make_float2(0.f, 0.f);
         bad |= out;
     }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
@@ -474,14 +472,12 @@ struct CgControl {
 
 __device__ __forceinline__ bool cg_done(const CgControl *c) { return c && *(volatile const int *)&c->done; }
 
-// Ap = A p with LANES lanes per block row: the lanes of a row read consecutive 3x3 blocks,
-// and a shuffle reduction sums their partial products. With dots, dots[0] += p . Ap.
-// Small systems are latency bound and take 8 lanes per row. Large ones take 4 in
-// double-float (coalesced block reads; the 513^2 cloth step was 2 % faster than with 1 lane
-// and 4 % faster than with 8) and 1 in FP64, where the FP64 pipe binds and the reduction's
-// extra adds would cost more than they hide.
+// Ap = A p in FP64 with LANES lanes per block row: the lanes of a row read consecutive 3x3
+// blocks, and a shuffle reduction sums their partial products. With dots, dots[0] += p . Ap.
+// This is the product of the FP64 CG (the fallback when the system leaves the double-float
+// range) and of the methods' K v terms. Small systems are latency bound and take 8 lanes per
+// row; large ones 1, where the FP64 pipe binds.
 constexpr int kSpmvLanesSmall = 8;
-constexpr int kSpmvLanesLarge = 4;
 constexpr int kSpmvSmallRows = 65536;
 constexpr int kSplitBlocks = 152 * 8;  // grid-stride split of the system matrix
 
@@ -509,92 +505,31 @@ __device__ __forceinline__ void df_add(float &sh, float &sl, float bh, float bl)
     sl = __fadd_rn(sl, __fadd_rn(e, bl));
 }
 
-// With p2 (the CG, when *T.wide is clear) the products and the lane reduction run in
-// double-float on T.val2 and p2, and lane 0 rounds the sums to FP64; otherwise everything runs
-// in FP64 on T.val and p. The choice is the same for the whole grid.
 template <int LANES>
 __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict__ p, double *Ap, int nv, double *dots,
-                                     const CgControl *ctl = nullptr, const float2 *__restrict__ p2 = nullptr)
+                                     const CgControl *ctl = nullptr)
 {
     if (cg_done(ctl)) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / LANES;
     const int lane = t & (LANES - 1);
     double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-    if (p2 && !*(volatile const int *)T.wide) {
-        float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
-        if (i < nv) {
-            const int k1 = __ldg(T.row_ptr + i + 1);
-#pragma unroll 2
-            const size_t nb = size_t(T.nnzb);
-            for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
-                const float2 *bl = T.val2 + k;
-                const float2 *x = p2 + 3 * size_t(__ldg(T.col + k));
-                const float2 x0 = x[0], x1 = x[1], x2 = x[2];
-                df_fma(h0, l0, __ldg(bl), x0);
-                df_fma(h0, l0, __ldg(bl + nb), x1);
-                df_fma(h0, l0, __ldg(bl + 2 * nb), x2);
-                df_fma(h1, l1, __ldg(bl + 3 * nb), x0);
-                df_fma(h1, l1, __ldg(bl + 4 * nb), x1);
-                df_fma(h1, l1, __ldg(bl + 5 * nb), x2);
-                df_fma(h2, l2, __ldg(bl + 6 * nb), x0);
-                df_fma(h2, l2, __ldg(bl + 7 * nb), x1);
-                df_fma(h2, l2, __ldg(bl + 8 * nb), x2);
-            }
+    if (i < nv) {
+        const int k1 = __ldg(T.row_ptr + i + 1);
+        for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
+            const double *bl = T.val + size_t(k) * 9;
+            const double *x = p + 3 * size_t(__ldg(T.col + k));
+            const double x0 = x[0], x1 = x[1], x2 = x[2];
+            y0 += bl[0] * x0 + bl[1] * x1 + bl[2] * x2;
+            y1 += bl[3] * x0 + bl[4] * x1 + bl[5] * x2;
+            y2 += bl[6] * x0 + bl[7] * x1 + bl[8] * x2;
         }
+    }
 #pragma unroll
-        for (int o = LANES / 2; o > 0; o >>= 1) {
-            df_add(h0, l0, __shfl_xor_sync(0xffffffffu, h0, o), __shfl_xor_sync(0xffffffffu, l0, o));
-            df_add(h1, l1, __shfl_xor_sync(0xffffffffu, h1, o), __shfl_xor_sync(0xffffffffu, l1, o));
-            df_add(h2, l2, __shfl_xor_sync(0xffffffffu, h2, o), __shfl_xor_sync(0xffffffffu, l2, o));
-        }
-        // p . Ap in double-float as well: lane 0 of each row forms its row's product, the
-        // warp reduces in double-float, and only the warp sums meet in FP64.
-        float ph = 0.f, pl = 0.f;
-        if (i < nv && lane == 0) {
-            Ap[3 * i] = double(h0) + double(l0);
-            Ap[3 * i + 1] = double(h1) + double(l1);
-            Ap[3 * i + 2] = double(h2) + double(l2);
-            if (dots) {
-                const float2 *pi = p2 + 3 * size_t(i);
-                df_fma(ph, pl, pi[0], make_float2(h0, l0));
-                df_fma(ph, pl, pi[1], make_float2(h1, l1));
-                df_fma(ph, pl, pi[2], make_float2(h2, l2));
-            }
-        }
-        if (dots) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                df_add(ph, pl, __shfl_xor_sync(0xffffffffu, ph, o), __shfl_xor_sync(0xffffffffu, pl, o));
-            __shared__ double part_df[32];
-            const int w = threadIdx.x >> 5;
-            if ((threadIdx.x & 31) == 0) part_df[w] = double(ph) + double(pl);
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                double sum = 0.0;
-                for (int k = 0; k < (blockDim.x + 31) / 32; ++k) sum += part_df[k];
-                atomicAdd(dots, sum);
-            }
-        }
-        return;
-    } else {
-        if (i < nv) {
-            const int k1 = __ldg(T.row_ptr + i + 1);
-            for (int k = __ldg(T.row_ptr + i) + lane; k < k1; k += LANES) {
-                const double *bl = T.val + size_t(k) * 9;
-                const double *x = p + 3 * size_t(__ldg(T.col + k));
-                const double x0 = x[0], x1 = x[1], x2 = x[2];
-                y0 += bl[0] * x0 + bl[1] * x1 + bl[2] * x2;
-                y1 += bl[3] * x0 + bl[4] * x1 + bl[5] * x2;
-                y2 += bl[6] * x0 + bl[7] * x1 + bl[8] * x2;
-            }
-        }
-#pragma unroll
-        for (int o = LANES / 2; o > 0; o >>= 1) {
-            y0 += __shfl_xor_sync(0xffffffffu, y0, o);
-            y1 += __shfl_xor_sync(0xffffffffu, y1, o);
-            y2 += __shfl_xor_sync(0xffffffffu, y2, o);
-        }
+    for (int o = LANES / 2; o > 0; o >>= 1) {
+        y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+        y1 += __shfl_xor_sync(0xffffffffu, y1, o);
+        y2 += __shfl_xor_sync(0xffffffffu, y2, o);
     }
     double pap = 0.0;
     if (i < nv && lane == 0) {
@@ -606,26 +541,22 @@ __global__ void implicit_spmv_kernel(ImplicitTables T, const double *__restrict_
     if (dots) block_reduce_add(pap, dots);
 }
 
-// One SpMV on the stream, with the lane count for the system's size.
+// One FP64 product on the stream, with the lane count for the system's size.
 static void launch_spmv(const ImplicitTables &T, const double *p, double *Ap, int nv, double *dots,
-                        const CgControl *ctl, cudaStream_t st, const float2 *p2 = nullptr)
+                        const CgControl *ctl, cudaStream_t st)
 {
     if (nv < kSpmvSmallRows)
         implicit_spmv_kernel<kSpmvLanesSmall>
-            <<<(nv * kSpmvLanesSmall + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl, p2);
-    else if (p2)
-        implicit_spmv_kernel<kSpmvLanesLarge>
-            <<<(nv * kSpmvLanesLarge + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl, p2);
+            <<<(nv * kSpmvLanesSmall + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl);
     else
-        implicit_spmv_kernel<1><<<(nv + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl, p2);
+        implicit_spmv_kernel<1><<<(nv + 255) / 256, 256, 0, st>>>(T, p, Ap, nv, dots, ctl);
 }
 
-// CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z (per component).
+// FP64 CG start with x = 0: r = b, z = D^-1 r, p = z; dots[1] += r.r, dots[2] += r.z.
 __global__ void implicit_cg_init_kernel(const double *b, const double *dinv, double *x, double *r, double *z,
-                                       double *p, float2 *p2, int *wide, int n, double *dots)
+                                       double *p, int n, double *dots)
 {
     double rr = 0.0, rz = 0.0;
-    bool bad = false;
 #pragma unroll 4
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double ri = b[i], zi = ri * dinv[i];
@@ -633,13 +564,9 @@ __global__ void implicit_cg_init_kernel(const double *b, const double *dinv, dou
         r[i] = ri;
         z[i] = zi;
         p[i] = zi;
-        bool o;
-        p2[i] = split_df(zi, o);
-        bad |= o;
         rr += ri * ri;
         rz += ri * zi;
     }
-    flag_wide(bad, wide);
     block_reduce_add2(rr, rz, dots + 1, dots + 2);
 }
 // Eigen's start: nothing to do for b = 0; otherwise iterate while |r|^2 >= tol^2 |b|^2.
@@ -681,8 +608,8 @@ __global__ void implicit_cg_update_kernel(double *x, double *r, double *z, const
 // The iteration's stopping test (Eigen: |r|^2 < thr2 after the update, or the iteration
 // limit), then p = z + beta p with beta = rz_new / rz_old. Every block takes the same
 // decision: its inputs were written by earlier kernels.
-__global__ void implicit_cg_direction_kernel(double *p, float2 *p2, int *wide, const double *z, int n,
-                                            const double *prev, const double *cur, CgControl *ctl)
+__global__ void implicit_cg_direction_kernel(double *p, const double *z, int n, const double *prev, const double *cur,
+                                            CgControl *ctl)
 {
     if (cg_done(ctl)) return;
     const double rr = cur[1];
@@ -698,17 +625,11 @@ __global__ void implicit_cg_direction_kernel(double *p, float2 *p2, int *wide, c
     if (threadIdx.x == 0) s_beta = cur[2] / prev[2];
     __syncthreads();
     const double beta = s_beta;
-    bool bad = false;
 #pragma unroll 4
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double pi = z[i] + beta * p[i];
-        p[i] = pi;
-        bool o;
-        p2[i] = split_df(pi, o);
-        bad |= o;
-    }
-    flag_wide(bad, wide);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
 }
+
+#include "implicit_cg.cuh"
 
 // ---- vector steps of the methods (n = 3 V degrees of freedom; mass per vertex) ------------
 
@@ -828,6 +749,75 @@ static int grid_of(int n, int t = 256) { return (n + t - 1) / t; }
 // reductions (a shuffle tree per thread) are paid once per few entries: 4 blocks of 256 per SM.
 static int cg_grid(int n) { return std::max(1, std::min(grid_of(n), 152 * 4)); }
 
+// Reverse Cuthill-McKee order of a graph given by adjacency lists (each sorted, the vertex
+// itself included): per component, breadth-first from a pseudo-peripheral vertex (George and
+// Liu's search: restart from a minimum-degree vertex of the last level while that deepens the
+// level structure), neighbours taken in increasing degree; the whole order is then reversed.
+// Returns each vertex's position. Vertices that share a block of the system matrix get
+// positions a few hundred apart on a cloth, which is what the symmetric product's transposed
+// reads need to find their blocks in L2.
+static std::vector<int32_t> rcm_positions(const std::vector<std::vector<int32_t>> &adj)
+{
+    const int n = static_cast<int>(adj.size());
+    auto deg = [&](int v) { return static_cast<int>(adj[v].size()); };
+    auto lighter = [&](int a, int b) { return deg(a) < deg(b) || (deg(a) == deg(b) && a < b); };
+    std::vector<int32_t> mark(n, -1), order, cur, next;
+    std::vector<char> placed(n, 0);
+    order.reserve(n);
+    int stamp = 0;
+    // Depth of the level structure rooted at s, and a minimum-degree vertex of its last level.
+    auto levels = [&](int s, int &far) {
+        ++stamp;
+        cur.assign(1, s);
+        mark[s] = stamp;
+        int depth = 0;
+        for (;;) {
+            next.clear();
+            for (int v : cur)
+                for (int u : adj[v])
+                    if (mark[u] != stamp) {
+                        mark[u] = stamp;
+                        next.push_back(u);
+                    }
+            if (next.empty()) break;
+            cur.swap(next);
+            ++depth;
+        }
+        far = *std::min_element(cur.begin(), cur.end(), lighter);
+        return depth;
+    };
+    for (int s = 0; s < n; ++s) {
+        if (placed[s]) continue;
+        int root = s, far = s;
+        int depth = levels(root, far);
+        for (int tries = 0; tries < 8; ++tries) {
+            int far2 = far;
+            const int d2 = levels(far, far2);
+            if (d2 <= depth) break;
+            root = far;
+            depth = d2;
+            far = far2;
+        }
+        const size_t first = order.size();
+        order.push_back(root);
+        placed[root] = 1;
+        std::vector<int32_t> nbrs;
+        for (size_t q = first; q < order.size(); ++q) {
+            nbrs.clear();
+            for (int u : adj[order[q]])
+                if (!placed[u]) nbrs.push_back(u);
+            std::sort(nbrs.begin(), nbrs.end(), lighter);
+            for (int u : nbrs) {
+                placed[u] = 1;
+                order.push_back(u);
+            }
+        }
+    }
+    std::vector<int32_t> pos(n);
+    for (int k = 0; k < n; ++k) pos[order[k]] = n - 1 - k;
+    return pos;
+}
+
 struct ImplicitSolver {
     SceneLayout L;
     spgx_implicit_params P{};
@@ -837,8 +827,14 @@ struct ImplicitSolver {
     DevBuf d_idx, d_info, d_prm, d_eblk, d_row, d_col, d_val, d_diag, d_mass;
     DevBuf d_x, d_v, d_x0, d_v0, d_vi, d_xm1, d_vm1, d_f, d_b, d_u, d_w;
     DevBuf d_dx, d_r, d_z, d_p, d_Ap, d_dinv, d_dots, d_ctl;
-    DevBuf d_val2, d_p2, d_wide;  // the CG's double-float matrix and direction, and the range flag
-    HostBuf h_dots, h_ctl, h_wide;
+    DevBuf d_wide;  // the matrix is out of double-float range
+    // The double-float CG: symmetric matrix, vectors, block partials and barrier state.
+    DevBuf d_urow, d_ucol, d_uval, d_ufull, d_lrow, d_lent;
+    DevBuf d_x2, d_r2, d_p2, d_Ap2, d_d2, d_part, d_sync;
+    HostBuf h_dots, h_ctl, h_sync;
+    CgSymDf SD{};
+    int cg_lanes{4}, cg_blocks{0};
+    std::vector<int32_t> row_of;  // the CG's row of each vertex (scene order over all objects)
     cudaGraphExec_t cg_graph{nullptr};
     ImplicitTables T{};
     int n_elem{0}, nnzb{0};
@@ -862,7 +858,8 @@ struct ImplicitSolver {
     static spgx_status check_params(const spgx_implicit_params *p)
     {
         if (!p || !(p->dt > 0) || p->substeps < 1 || !(p->cg_threshold >= 0) || p->cg_max_iterations < 0 ||
-            p->method < SPGX_IMPLICIT_NEWTON_DX || p->method > SPGX_SYMPLECTIC_EULER) {
+            p->method < SPGX_IMPLICIT_NEWTON_DX || p->method > SPGX_SYMPLECTIC_EULER || p->cg_precision < 0 ||
+            p->cg_precision > 1) {
             set_error("invalid implicit solver parameters");
             return SPGX_ERR_INVALID_ARG;
         }
@@ -900,8 +897,8 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         SPGX_CUDA(cudaEventCreate(&ev0));
         SPGX_CUDA(cudaEventCreate(&ev1));
-        // Element list over every energy (internal vertex ids), the block pattern and the FP64
-        // masses in internal order.
+        // Element list over every energy and the vertex adjacency (scene vertex ids: object
+        // base + vertex), then the rows in reverse Cuthill-McKee order of that adjacency.
         const int nv = L.nv;
         std::vector<I4> idx, info;
         std::vector<double> prm, mass(std::max(1, nv), 0.0);
@@ -910,13 +907,12 @@ struct ImplicitSolver {
         for (int o = 0; o < scene->n_objects; ++o) {
             const auto &ob = scene->objects[o];
             const int vb = L.objects[o].vertex_base;
-            for (int k = 0; k < ob.n_vertices; ++k) mass[L.ext2int[vb + k]] = ob.mass[k];
             for (int e = 0; e < ob.n_energies; ++e) {
                 const auto &E = ob.energies[e];
                 const int S = stencil_size(E.type), Pc = param_count(E.type);
                 for (int s = 0; s < E.n_stencils; ++s) {
                     int iv[4] = {-1, -1, -1, -1};
-                    for (int k = 0; k < S; ++k) iv[k] = L.ext2int[vb + E.stencils[int64_t(s) * S + k]];
+                    for (int k = 0; k < S; ++k) iv[k] = vb + E.stencils[int64_t(s) * S + k];
                     idx.push_back({iv[0], iv[1], iv[2], iv[3]});
                     info.push_back({E.type, static_cast<int32_t>(prm.size()), S, 0});
                     for (int k = 0; k < Pc; ++k) prm.push_back(E.params[int64_t(s) * Pc + k]);
@@ -926,13 +922,33 @@ struct ImplicitSolver {
                 }
             }
         }
+        for (auto &r : nb) {
+            std::sort(r.begin(), r.end());
+            r.erase(std::unique(r.begin(), r.end()), r.end());
+        }
+        row_of = rcm_positions(nb);
+        for (int o = 0; o < scene->n_objects; ++o) {
+            const int vb = L.objects[o].vertex_base;
+            for (int k = 0; k < scene->objects[o].n_vertices; ++k) mass[row_of[vb + k]] = scene->objects[o].mass[k];
+        }
+        for (auto &e : idx) {
+            int *iv[4] = {&e.x, &e.y, &e.z, &e.w};
+            for (int *v : iv)
+                if (*v >= 0) *v = row_of[*v];
+        }
+        {
+            std::vector<std::vector<int32_t>> by_row(nv);
+            for (int v = 0; v < nv; ++v) {
+                auto &r = by_row[row_of[v]];
+                for (int u : nb[v]) r.push_back(row_of[u]);
+                std::sort(r.begin(), r.end());
+            }
+            nb.swap(by_row);
+        }
         n_elem = static_cast<int>(idx.size());
         std::vector<int32_t> row(nv + 1, 0), col, diag(nv);
         for (int v = 0; v < nv; ++v) {
-            auto &r = nb[v];
-            std::sort(r.begin(), r.end());
-            r.erase(std::unique(r.begin(), r.end()), r.end());
-            for (int c : r) {
+            for (int c : nb[v]) {
                 if (c == v) diag[v] = static_cast<int32_t>(col.size());
                 col.push_back(c);
             }
@@ -964,24 +980,76 @@ struct ImplicitSolver {
         SPGX_TRY_STATUS(d_diag.upload(diag.empty() ? std::vector<int32_t>{0} : diag));
         SPGX_TRY_STATUS(d_mass.upload(mass));
         SPGX_TRY_STATUS(d_val.alloc(size_t(std::max(1, nnzb)) * 9 * sizeof(double)));
+        // The CG's symmetric pattern: row i's upper blocks are the tail of its full row from the
+        // diagonal on; its lower block (i, j) is read as the transpose of the stored (j, i).
+        {
+            std::vector<int32_t> urow(nv + 1, 0), ucol, ufull, lrow(nv + 1, 0), lent;
+            for (int i = 0; i < nv; ++i) {
+                for (int f = diag[i]; f < row[i + 1]; ++f) {
+                    ucol.push_back(col[f]);
+                    ufull.push_back(f);
+                }
+                urow[i + 1] = static_cast<int32_t>(ucol.size());
+            }
+            for (int i = 0; i < nv; ++i) {
+                for (int f = row[i]; f < diag[i]; ++f) {
+                    const int j = col[f];
+                    const int fji = static_cast<int>(std::lower_bound(col.begin() + row[j], col.begin() + row[j + 1], i) -
+                                                     col.begin());
+                    lent.push_back(j);
+                    lent.push_back(urow[j] + (fji - diag[j]));
+                }
+                lrow[i + 1] = static_cast<int32_t>(lent.size() / 2);
+            }
+            SD.nnzu = static_cast<int>(ucol.size());
+            if (ucol.empty()) {
+                ucol.push_back(0);
+                ufull.push_back(0);
+            }
+            if (lent.empty()) lent.assign(2, 0);
+            SPGX_TRY_STATUS(d_urow.upload(urow));
+            SPGX_TRY_STATUS(d_ucol.upload(ucol));
+            SPGX_TRY_STATUS(d_ufull.upload(ufull));
+            SPGX_TRY_STATUS(d_lrow.upload(lrow));
+            SPGX_TRY_STATUS(d_lent.upload(lent));
+            SPGX_TRY_STATUS(d_uval.alloc(size_t(std::max(1, SD.nnzu)) * kCgBlockFloat4 * sizeof(float4)));
+            SD.urow = d_urow.as<int>();
+            SD.ucol = d_ucol.as<int>();
+            SD.ublk = d_uval.as<float4>();
+            SD.lrow = d_lrow.as<int>();
+            SD.lent = d_lent.as<int2>();
+        }
         const size_t vb = size_t(std::max(1, nv)) * 3 * sizeof(double);
         for (DevBuf *b : {&d_x, &d_v, &d_x0, &d_v0, &d_vi, &d_xm1, &d_vm1, &d_f, &d_b, &d_u, &d_w, &d_dx, &d_r, &d_z,
                           &d_p, &d_Ap, &d_dinv})
             SPGX_TRY_STATUS(b->alloc(vb));
-        SPGX_TRY_STATUS(d_val2.alloc(size_t(std::max(1, nnzb)) * 9 * sizeof(float2)));
-        SPGX_TRY_STATUS(d_p2.alloc(size_t(std::max(1, nv)) * 3 * sizeof(float2)));
+        for (DevBuf *b : {&d_x2, &d_r2, &d_p2, &d_Ap2, &d_d2})
+            SPGX_TRY_STATUS(b->alloc(size_t(std::max(1, nv)) * 2 * sizeof(float4)));
         SPGX_TRY_STATUS(d_wide.alloc(sizeof(int)));
+        SPGX_TRY_STATUS(d_sync.alloc(sizeof(CgSync)));
+        SPGX_TRY_STATUS(h_sync.alloc(sizeof(CgSync)));
+        // The CG's launch shape: one lane per row on large systems (the fewest dependent
+        // memory round trips per warp), 8 on small ones (latency bound, few rows to spread); as
+        // many co-resident blocks as fit and the rows need (one per SM).
+        {
+            cg_lanes = nv < kSpmvSmallRows ? 8 : 4;
+            int per_sm = 0, sms = 0;
+            SPGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, cg_lanes == 8 ? implicit_cg_df_kernel<8> : implicit_cg_df_kernel<4>, kCgThreads, 0));
+            SPGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+            const long long need = (std::max<long long>(3LL * nv, 1LL * nv * cg_lanes) + kCgThreads - 1) / kCgThreads;
+            cg_blocks = static_cast<int>(std::max(1LL, std::min<long long>(need, 1LL * std::max(1, per_sm) * sms)));
+            SPGX_TRY_STATUS(d_part.alloc(size_t(cg_blocks) * 2 * 4 * sizeof(double)));
+        }
         SPGX_TRY_STATUS(d_dots.alloc(size_t(8) * sizeof(double)));
         SPGX_TRY_STATUS(h_dots.alloc(size_t(8) * sizeof(double)));
         SPGX_TRY_STATUS(d_ctl.alloc(sizeof(CgControl)));
         SPGX_TRY_STATUS(h_ctl.alloc(sizeof(CgControl)));
-        SPGX_TRY_STATUS(h_wide.alloc(sizeof(int)));
         T = ImplicitTables{d_idx.as<int4>(), d_info.as<int4>(), d_prm.as<double>(), d_eblk.as<int>(), d_row.as<int>(),
-                           d_col.as<int>(), d_val.as<double>(), d_diag.as<int>(), d_val2.as<float2>(),
-                           d_wide.as<int>(), nnzb};
+                           d_col.as<int>(), d_val.as<double>(), d_diag.as<int>(), d_wide.as<int>(), nnzb};
         std::vector<double> x(3 * size_t(std::max(1, nv)), 0.0), v(x.size(), 0.0);
         for (int i = 0; i < nv; ++i) {
-            const int k = L.ext2int[i];
+            const int k = row_of[i];
             for (int a = 0; a < 3; ++a) {
                 x[3 * size_t(k) + a] = L.x_ext[3 * size_t(i) + a];
                 v[3 * size_t(k) + a] = L.v_ext[3 * size_t(i) + a];
@@ -1019,11 +1087,9 @@ struct ImplicitSolver {
         return SPGX_OK;
     }
 
-    // One CG solve of (alpha M + beta H) d_dx = d_b (ImplicitEulerBase::solveLinearSystem,
-    // implicitEulerBase.cpp:227-239) with Eigen::ConjugateGradient's stopping rule
-    // |r|^2 < tol^2 |b|^2. The BSR holds H on entry.
-    // The CG iterations as one graph of kCgChunk iterations (two parities of the dot-product
-    // slots per pair of iterations), replayed until the device-side control says done.
+    // The FP64 CG's iterations as one graph of kCgChunk iterations (two parities of the
+    // dot-product slots per pair of iterations), replayed until the device-side control says
+    // done.
     static constexpr int kCgChunk = 32;
     spgx_status build_cg_graph()
     {
@@ -1035,12 +1101,11 @@ struct ImplicitSolver {
         for (int it = 0; it < kCgChunk; ++it) {
             double *prev = it % 2 == 0 ? A : B, *cur = it % 2 == 0 ? B : A;
             cudaMemsetAsync(prev, 0, sizeof(double), stream);
-            launch_spmv(T, vec(d_p), vec(d_Ap), nv, prev, ctl, stream, d_p2.as<float2>());
+            launch_spmv(T, vec(d_p), vec(d_Ap), nv, prev, ctl, stream);
             cudaMemsetAsync(cur, 0, 3 * sizeof(double), stream);
             implicit_cg_update_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_dx), vec(d_r), vec(d_z), vec(d_p),
                                                                      vec(d_Ap), vec(d_dinv), n, prev, cur, ctl);
-            implicit_cg_direction_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_p), d_p2.as<float2>(), T.wide,
-                                                                        vec(d_z), n, prev, cur, ctl);
+            implicit_cg_direction_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_p), vec(d_z), n, prev, cur, ctl);
         }
         const cudaError_t ce = cudaStreamEndCapture(stream, &g);
         if (ce != cudaSuccess) {
@@ -1058,17 +1123,63 @@ struct ImplicitSolver {
 
     // One CG solve of (alpha M + beta H) d_dx = d_b (ImplicitEulerBase::solveLinearSystem,
     // implicitEulerBase.cpp:227-239) with Eigen::ConjugateGradient's stopping rule
-    // |r|^2 < tol^2 |b|^2. The BSR holds H on entry.
+    // |r|^2 < tol^2 |b|^2. The BSR holds H on entry. The solve runs in double-float as one
+    // cooperative launch; when the system leaves that range it runs again in FP64.
     spgx_status cg(double alpha, double beta, int &iterations, double &rel_residual)
     {
         const int nv = L.nv, n = n3();
         implicit_lhs_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_mass), nv, alpha, beta, vec(d_dinv));
+        if (P.cg_precision == 1) return cg_fp64(iterations, rel_residual);
         SPGX_CUDA(cudaMemsetAsync(T.wide, 0, sizeof(int), stream));
-        implicit_split_kernel<<<kSplitBlocks, 256, 0, stream>>>(T, size_t(nnzb) * 9, nv);
+        implicit_split_kernel<<<kSplitBlocks, 256, 0, stream>>>(T, d_uval.as<float2>(), d_ufull.as<int>(), SD.nnzu, nv);
+        SPGX_CUDA(cudaMemsetAsync(d_sync.as<void>(), 0, sizeof(CgSync), stream));
+        SPGX_CUDA(cudaGetLastError());
+        CgDfVecs V{vec(d_b), vec(d_dinv), vec(d_dx), d_x2.as<float4>(), d_r2.as<float4>(), d_p2.as<float4>(),
+                   d_Ap2.as<float4>(), d_d2.as<float4>(), d_part.as<double>(), n, nv};
+        CgSync *sync = d_sync.as<CgSync>();
+        CgControl *ctl = d_ctl.as<CgControl>();
+        const int *wide = T.wide;
+        const double tol = P.cg_threshold;
+        int max_its = P.cg_max_iterations;
+        void *args[] = {&SD, &V, &sync, &ctl, &wide, const_cast<double *>(&tol), &max_its};
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(cg_blocks);
+        cfg.blockDim = dim3(kCgThreads);
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SPGX_CUDA(cudaLaunchKernelExC(&cfg,
+                                      cg_lanes == 8 ? reinterpret_cast<const void *>(implicit_cg_df_kernel<8>)
+                                                    : reinterpret_cast<const void *>(implicit_cg_df_kernel<4>),
+                                      args));
+        SPGX_CUDA(cudaMemcpyAsync(h_ctl.as<void>(), ctl, sizeof(CgControl), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaMemcpyAsync(h_sync.as<void>(), sync, sizeof(CgSync), cudaMemcpyDeviceToHost, stream));
+        SPGX_CUDA(cudaStreamSynchronize(stream));
+        const CgControl *hc = h_ctl.as<CgControl>();
+        const int status = h_sync.as<CgSync>()->status;
+        if (status == kCgTimeout) {
+            set_error("a grid barrier of the CG solve gave up waiting");
+            return SPGX_ERR_TIMEOUT;
+        }
+        if (status == kCgOutOfRange) return cg_fp64(iterations, rel_residual);
+        fp64_products = false;
+        iterations = hc->its;
+        rel_residual = hc->rr0 > 0.0 ? std::sqrt(hc->rr / hc->rr0) : 0.0;
+        return SPGX_OK;
+    }
+
+    // The FP64 CG on the full pattern, for systems outside the double-float range; the system
+    // matrix and preconditioner are already in place.
+    spgx_status cg_fp64(int &iterations, double &rel_residual)
+    {
+        const int n = n3();
         double *dots = d_dots.as<double>();  // two sets of {pAp, rr, rz}: [0..2] and [3..5]
         SPGX_CUDA(cudaMemsetAsync(dots, 0, 6 * sizeof(double), stream));
         implicit_cg_init_kernel<<<cg_grid(n), 256, 0, stream>>>(vec(d_b), vec(d_dinv), vec(d_dx), vec(d_r), vec(d_z),
-                                                                vec(d_p), d_p2.as<float2>(), T.wide, n, dots);
+                                                                vec(d_p), n, dots);
         implicit_cg_control_kernel<<<1, 1, 0, stream>>>(d_ctl.as<CgControl>(), dots, P.cg_threshold,
                                                         P.cg_max_iterations);
         SPGX_CUDA(cudaGetLastError());
@@ -1086,15 +1197,13 @@ struct ImplicitSolver {
             set_error("internal: the CG control did not finish");
             return SPGX_ERR_CUDA;
         }
-        SPGX_CUDA(cudaMemcpyAsync(h_wide.as<void>(), T.wide, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        SPGX_CUDA(cudaStreamSynchronize(stream));
-        fp64_products = *h_wide.as<int>() != 0;
+        fp64_products = true;
         iterations = hc->its;
         rel_residual = hc->rr0 > 0.0 ? std::sqrt(hc->rr / hc->rr0) : 0.0;
         return SPGX_OK;
     }
 
-    bool fp64_products{false};  // the last solve's products ran in FP64 (out of double-float range)
+    bool fp64_products{false};  // the last solve ran in FP64 (out of double-float range)
 
     struct Tally {
         int cg_iterations = 0, newton_iterations = 0, failed = 0, fp64_solves = 0;
@@ -1368,7 +1477,7 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaStreamSynchronize(stream));
         const auto &O = L.objects[obj];
         for (int k = 0; k < O.nv; ++k) {
-            const size_t i = size_t(L.ext2int[O.vertex_base + k]);
+            const size_t i = size_t(row_of[O.vertex_base + k]);
             for (int a = 0; a < 3; ++a) {
                 if (x) x[3 * k + a] = hx[3 * i + a];
                 if (v) v[3 * k + a] = hv[3 * i + a];
@@ -1390,7 +1499,7 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaStreamSynchronize(stream));
         const auto &O = L.objects[obj];
         for (int k = 0; k < O.nv; ++k) {
-            const size_t i = size_t(L.ext2int[O.vertex_base + k]);
+            const size_t i = size_t(row_of[O.vertex_base + k]);
             for (int a = 0; a < 3; ++a) {
                 if (x) hx[3 * i + a] = x[3 * k + a];
                 if (v) hv[3 * i + a] = v[3 * k + a];
@@ -1441,6 +1550,7 @@ void spgx_implicit_params_default(spgx_implicit_params *p)
     p->cg_max_iterations = 300;
     p->device = 0;
     p->method = SPGX_IMPLICIT_NEWTON_DX;
+    p->cg_precision = 0;
 }
 
 spgx_status spgx_implicit_create(const spgx_scene_desc *scene, const spgx_implicit_params *params, spgx_implicit **out)

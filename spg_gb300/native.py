@@ -65,7 +65,7 @@ class XpbdParams(C.Structure):
 class ImplicitParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("substeps", C.c_int32), ("gravity", C.c_double * 3),
                 ("cg_threshold", C.c_double), ("cg_max_iterations", C.c_int32), ("device", C.c_int32),
-                ("method", C.c_int32)]
+                ("method", C.c_int32), ("cg_precision", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -405,7 +405,7 @@ class ImplicitSolver:
     QUASI_STATIC_NEWTON_ROBUST and SYMPLECTIC_EULER."""
 
     def __init__(self, objects, dt=0.01, substeps=1, gravity=(0.0, -9.8, 0.0), cg_threshold=1e-5,
-                 cg_max_iterations=300, device=0, method=NEWTON_DX):
+                 cg_max_iterations=300, device=0, method=NEWTON_DX, cg_precision=0):
         self.objects_nv = [len(np.asarray(o.mass).reshape(-1)) for o in objects]
         self._d = Descriptor(objects)
         p = ImplicitParams()
@@ -413,7 +413,7 @@ class ImplicitSolver:
         p.dt, p.substeps = dt, substeps
         p.gravity = (C.c_double * 3)(*gravity)
         p.cg_threshold, p.cg_max_iterations, p.device = cg_threshold, cg_max_iterations, device
-        p.method = method
+        p.method, p.cg_precision = method, cg_precision
         self.params = p
         h = C.c_void_p()
         check(lib().spgx_implicit_create(C.byref(self._d.scene), C.byref(p), C.byref(h)))

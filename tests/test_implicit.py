@@ -126,6 +126,75 @@ def test_wide_system_runs_fp64_products():
     assert np.abs(xw - xb).max() <= 1e-3 * moved
 
 
+def _pinned_spring_cloth(n):
+    """A spring cloth with the large-cloth spacing (2 m at 513 vertices per side, k 1e4, no
+    jitter) under a soft pin (k 50) at every vertex, started from a 1 cm out-of-plane wave:
+    every spring is stretched, so the Newton system is positive definite and the FP64 oracle
+    well conditioned (a 1e-9 m perturbation of the start moves its result by 3e-10 m; about 60
+    CG iterations per step). 66,049 rows at n = 257, above the 65,536 from which the CG takes
+    4 lanes per row."""
+    w = 2.0 * (n - 1) / 512
+    obj = O.build_spring_cloth(0.1 * w * w, w, w, n, n, 1e4, 1e-4, 1e5, 0.0, 7)
+    nv = obj.x.shape[0]
+    pins = np.concatenate([obj.x0, np.full((nv, 1), 50.0), np.full((nv, 1), 1 / 50.0)], axis=1)  # [a, k, 1/k]
+    obj.energies.append(scenes._energy(O.ANCHOR, np.arange(nv, dtype=np.int32).reshape(-1, 1), pins))
+    obj.x = obj.x0 + np.stack([np.zeros(nv), np.zeros(nv), 0.01 * np.sin(3.0 * obj.x0[:, 0])], 1)
+    return obj
+
+
+@pytest.mark.gpu
+@pytest.mark.slow
+def test_large_system_matches_oracle():
+    """The double-float CG with 4 lanes per row (symmetric product, reverse Cuthill-McKee rows)
+    against the FP64 oracle, two steps of the pinned 257x257 cloth."""
+    N = pytest.importorskip("spg_gb300.native")
+    obj = _pinned_spring_cloth(257)
+    assert obj.x.shape[0] >= 65536
+    gpu = N.ImplicitSolver([obj], dt=1 / 120, substeps=1, gravity=scenes.GRAVITY)
+    ref = IR.ImplicitEuler(obj, 1 / 120, 1, scenes.GRAVITY)
+    its = []
+    for _ in range(2):
+        st = gpu.step()
+        ref.step()
+        its.append((int(st.iterations), ref.last_iterations))
+        assert st.warm_accepted == 0  # the double-float solve, not the FP64 fallback
+    xg, _ = gpu.state(0)
+    xr, _ = ref.state()
+    moved = float(np.abs(xr - obj.x).max())
+    err = float(np.abs(xg - xr).max())
+    print(f"pinned 257x257 cloth: max |dx| {err:.3g} m after 2 steps (moved {moved:.3g} m); CG iterations "
+          f"GPU/oracle {its}")
+    assert err <= 1e-4 * moved
+    for a, b in its:
+        assert abs(a - b) <= max(2, b // 20)
+
+
+@pytest.mark.gpu
+@pytest.mark.slow
+def test_double_float_cg_matches_fp64_cg_at_513():
+    """The pinned cloth at 513x513 (263,169 vertices, the benchmark cloth's size): two Newton-Dx
+    steps with the double-float CG against the same steps with the FP64 CG (cg_precision 1).
+    At this size a thread of the CG launch owns more degrees of freedom than it keeps in
+    registers, so the direction's memory path runs as well."""
+    N = pytest.importorskip("spg_gb300.native")
+    obj = _pinned_spring_cloth(513)
+    out = []
+    for prec in (0, 1):
+        gpu = N.ImplicitSolver([obj], dt=1 / 120, substeps=1, gravity=scenes.GRAVITY, cg_precision=prec)
+        its = [(int(st.iterations), int(st.warm_accepted)) for st in (gpu.step(), gpu.step())]
+        out.append((gpu.state(0)[0], its))
+        gpu.close()
+    (x_df, it_df), (x_64, it_64) = out
+    moved = float(np.abs(x_64 - obj.x).max())
+    err = float(np.abs(x_df - x_64).max())
+    print(f"pinned 513x513 cloth, two steps: double-float vs FP64 CG max |dx| {err:.3g} m (moved {moved:.3g} m); "
+          f"(iterations, FP64 solves) {it_df} / {it_64}")
+    assert [w for _, w in it_df] == [0, 0] and [w for _, w in it_64] == [1, 1]
+    assert err <= 1e-4 * moved
+    for (a, _), (b, _) in zip(it_df, it_64):
+        assert a < 300 and abs(a - b) <= max(2, b // 20)
+
+
 # ---------------------------------------------------------------------------------------
 # The other global solvers (NewtonDv, NewtonRobust, BaraffWitkin, BDF2, StaticNewton,
 # QuasiStaticNewton, QuasiStaticNewtonRobust, SimplecticEuler), each on scenes where the
