@@ -349,7 +349,7 @@ def other_configs(local, only=None) -> dict:
         peak, peak_kind = _measured_peaks()
         alg = xpbd_algorithmic_bytes_per_substep(big)
         entry = {}
-        for kernel, name in ((2, "dataflow"), (1, "phase_launches")):
+        for kernel, name in ((3, "synchronised"), (2, "dataflow"), (1, "phase_launches")):
             x = N.XpbdSolver([big], dt=DT, substeps=20, gravity=GRAVITY, device=local, kernel=kernel)
             ms = statistics.mean(_timed_steps(x, 5))
             achieved = alg * 20 / (ms * 1e-3) / 1e9

@@ -463,8 +463,10 @@ typedef struct spgx_xpbd_params {
                          * launch, where a chunk of a phase starts once the chunks of earlier
                          * phases that touch its vertices have finished (same result, bit for
                          * bit; slower on the 513x513 cloth, whose chain of about 28 phases per
-                         * substep it runs task by task). A dataflow wait that runs out returns
-                         * SPGX_ERR_TIMEOUT. */
+                         * substep it runs task by task); 3 = synchronised: every substep of a
+                         * step in one persistent cooperative launch with a grid barrier after
+                         * each phase (same result, bit for bit). A wait of kernel 2 or 3 that
+                         * runs out returns SPGX_ERR_TIMEOUT. */
 } spgx_xpbd_params;
 
 void spgx_xpbd_params_default(spgx_xpbd_params *p);
@@ -475,10 +477,11 @@ spgx_status spgx_xpbd_step(spgx_xpbd *h, spgx_step_stats *stats);
 spgx_status spgx_xpbd_get_state(spgx_xpbd *h, int32_t object, double *x, double *v);
 spgx_status spgx_xpbd_set_state(spgx_xpbd *h, int32_t object, const double *x, const double *v);
 spgx_status spgx_xpbd_reset(spgx_xpbd *h);
-/* Failure-detection test hook (dataflow kernel only): marks one chunk's substep counter as
- * never reached, so that the next step's waits on it run out their bounded polls (about a
- * second). The step returns SPGX_ERR_TIMEOUT, the counters are reset and the handle keeps
- * working; nothing faults or hangs. */
+/* Failure-detection test hook (kernels 2 and 3): with kernel 2 it marks one chunk's substep
+ * counter as never reached, with kernel 3 it starts the next launch's grid barrier counter
+ * where no barrier completes, so that the next step's waits run out their bounded polls
+ * (about a second). The step returns SPGX_ERR_TIMEOUT, the counters are reset and the handle
+ * keeps working; nothing faults or hangs. */
 spgx_status spgx_xpbd_test_stall(spgx_xpbd *h);
 /* Stencil colours of one energy (colorStencils, graphColoring.cpp:51-70). */
 spgx_status spgx_xpbd_get_stencil_colors(spgx_xpbd *h, int32_t object, int32_t energy, int32_t *colors);

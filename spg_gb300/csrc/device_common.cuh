@@ -135,6 +135,42 @@ __device__ __forceinline__ int ld_relaxed_gpu(const int *p)
     return v;
 }
 
+// Release add to a grid barrier's counter: the arriving CTA's writes (its threads' writes
+// before the CTA barrier) are released with it.
+__device__ __forceinline__ void red_add_release_gpu(int *p, int v)
+{
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier number gen (counted from 0 within a cooperative launch): every CTA adds 1 to
+// *arrive (zeroed before the launch) and waits until gridDim.x (gen + 1) arrivals have been
+// counted; the acquire and the CTA barrier that follows make every CTA's earlier writes
+// visible to all threads of this one. The wait is bounded (max_polls sleeps of 32 ns plus an
+// L2 round trip each): one that runs out sets *status to timeout_code and the barrier returns
+// false in every thread of this CTA.
+__device__ __forceinline__ bool grid_counter_sync(int *arrive, int *status, int &gen, int max_polls, int timeout_code)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        red_add_release_gpu(arrive, 1);
+        const int target = (gen + 1) * int(gridDim.x);
+        int polls = 0, ok = 1;
+        while (ld_acquire_gpu(arrive) < target) {
+            if (++polls > max_polls) {
+                atomicExch(status, timeout_code);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        s_ok = ok;
+    }
+    ++gen;
+    __syncthreads();
+    return s_ok != 0;
+}
+
 
 // Walks the vertex's class-sorted incidence list with G lanes per vertex (lane-strided) and
 // accumulates the force and Hessian block of every incident element into acc; with kGeneric

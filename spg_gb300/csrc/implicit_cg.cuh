@@ -145,32 +145,10 @@ __device__ __forceinline__ void cg_block_partials(float2 a, float2 b, float2 c, 
     }
 }
 
-// Release add to a grid barrier's counter: the arriving block's writes (its threads' writes
-// before the CTA barrier) are released with it.
-__device__ __forceinline__ void red_add_release_gpu(int *p, int v)
-{
-    asm volatile("red.release.gpu.global.add.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
-}
-
-// Grid barrier number gen (counted from 0 within the launch): every block adds 1 and waits
-// until gridDim.x (gen + 1) arrivals have been counted. A wait that runs out sets kCgTimeout.
+// Grid barrier number gen of the CG launch (grid_counter_sync on the solve's counter).
 __device__ __forceinline__ void cg_grid_sync(CgSync *s, int &gen)
 {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        red_add_release_gpu(&s->arrive, 1);
-        const int target = (gen + 1) * int(gridDim.x);
-        int polls = 0;
-        while (ld_acquire_gpu(&s->arrive) < target) {
-            if (++polls > kCgMaxPolls) {
-                atomicExch(&s->status, kCgTimeout);
-                break;
-            }
-            __nanosleep(32);
-        }
-    }
-    ++gen;
-    __syncthreads();
+    grid_counter_sync(&s->arrive, &s->status, gen, kCgMaxPolls, kCgTimeout);
 }
 
 __device__ __forceinline__ int cg_status(const CgSync *s) { return vload(&s->status); }

@@ -50,12 +50,14 @@ def test_stall_hook_needs_the_dataflow_kernel():
         s.test_stall_tile(0)
 
 
-def test_xpbd_dataflow_wait_runs_out_and_the_solver_recovers():
-    """The XPBD dataflow kernel's bounded waits: a chunk counter that no substep reaches makes
-    the step return a timeout status; restored to the state before that step, the handle steps
-    exactly like a twin that never stalled."""
+@pytest.mark.parametrize("kernel", [2, 3])
+def test_xpbd_persistent_wait_runs_out_and_the_solver_recovers(kernel):
+    """The XPBD persistent kernels' bounded waits: a chunk counter that no substep reaches
+    (dataflow kernel) or a grid barrier counter that no barrier reaches (synchronised kernel)
+    makes the step return a timeout status; restored to the state before that step, the handle
+    steps exactly like a twin that never stalled."""
     obj = scenes.spring_cloth_cfg3(65)
-    kw = dict(dt=1 / 120, substeps=10, gravity=scenes.GRAVITY, kernel=2)
+    kw = dict(dt=1 / 120, substeps=10, gravity=scenes.GRAVITY, kernel=kernel)
     s = N.XpbdSolver([obj], **kw)
     twin = N.XpbdSolver([obj], **kw)
     s.step()

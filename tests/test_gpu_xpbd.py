@@ -33,10 +33,12 @@ def test_xpbd_positions(scene):
     assert err <= 1e-4 * extent
 
 
+@pytest.mark.parametrize("kernel", [2, 3])
 @pytest.mark.parametrize("scene", ["springs", "cloth", "beam", "membranes"])
-def test_dataflow_equals_phase_launches(scene):
-    """The dataflow XPBD kernel (every substep in one launch, chunks ordered by their vertex
-    chains) performs the same projections in the same per-vertex order as one launch per
+def test_persistent_kernels_equal_phase_launches(scene, kernel):
+    """The dataflow XPBD kernel (2: every substep in one launch, chunks ordered by their vertex
+    chains) and the synchronised one (3: every substep in one launch, a grid barrier between
+    phases) perform the same projections in the same per-vertex order as one launch per
     (energy, stencil colour) phase, so positions and velocities agree bit for bit."""
     if scene == "springs":
         obj, dt = scenes.spring_cloth_cfg3(129), 1 / 120
@@ -48,7 +50,7 @@ def test_dataflow_equals_phase_launches(scene):
         obj, dt = scenes.cloth_variant((O.CHOI_MEMBRANE, O.QUAD_BENDING), 17), 1 / 60
     kw = dict(dt=dt, substeps=20, gravity=scenes.GRAVITY)
     a = N.XpbdSolver([obj], kernel=1, **kw)
-    b = N.XpbdSolver([obj], kernel=2, **kw)
+    b = N.XpbdSolver([obj], kernel=kernel, **kw)
     for _ in range(3):
         a.step()
         b.step()
@@ -57,10 +59,11 @@ def test_dataflow_equals_phase_launches(scene):
     assert np.array_equal(xa, xb) and np.array_equal(va, vb)
 
 
-def test_dataflow_batch_of_objects():
-    """Several objects in one dataflow launch, each against its own oracle instance."""
+@pytest.mark.parametrize("kernel", [2, 3])
+def test_persistent_kernels_batch_of_objects(kernel):
+    """Several objects in one persistent launch, each against its own oracle instance."""
     objs = scenes.patch_batch_cfg4(5, 8, 16, seed=3)
-    gpu = N.XpbdSolver(objs, dt=1 / 60, substeps=10, gravity=scenes.GRAVITY, kernel=2)
+    gpu = N.XpbdSolver(objs, dt=1 / 60, substeps=10, gravity=scenes.GRAVITY, kernel=kernel)
     refs = [O.Xpbd(o, 1 / 60, 10, scenes.GRAVITY) for o in objs]
     for _ in range(3):
         gpu.step()
