@@ -501,13 +501,16 @@ class XpbdSolver:
         check(lib().spgx_xpbd_get_state(self.h, obj, _p(x, C.c_double), _p(v, C.c_double)))
         return x, v
 
+    def get_state_into(self, obj, x, v=None):
+        check(lib().spgx_xpbd_get_state(self.h, obj, _p(x, C.c_double), None if v is None else _p(v, C.c_double)))
+
     def set_state(self, obj, x, v=None):
         x = np.ascontiguousarray(x, dtype=np.float64)
         vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         check(lib().spgx_xpbd_set_state(self.h, obj, _p(x, C.c_double), None if vv is None else _p(vv, C.c_double)))
 
     def test_stall(self):
-        """Failure-detection test hook: the next dataflow step's waits on one chunk run out."""
+        """Failure-detection test hook: the next persistent step's bounded waits run out."""
         check(lib().spgx_xpbd_test_stall(self.h))
 
     def stencil_colors(self, obj, energy):

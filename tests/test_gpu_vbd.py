@@ -250,3 +250,34 @@ def test_autotuned_tile_size(kernel):
         a.step()
         ref.step()
     assert np.array_equal(a.state(0)[0], ref.state(0)[0])
+
+
+@pytest.mark.parametrize("solver", ["vbd", "xpbd"])
+def test_pinned_and_pageable_host_state_agree(solver):
+    """State moved through host arrays pinned by CUDA (asynchronous copies) and through
+    pageable arrays gives the same device state and the same host arrays, bit for bit."""
+    torch = pytest.importorskip("torch")
+    obj = scenes.spring_cloth_cfg3(65)
+    nv = obj.x.shape[0]
+    rng = np.random.default_rng(7)
+    x = obj.x + rng.normal(scale=1e-3, size=obj.x.shape)
+    v = rng.normal(scale=1e-2, size=obj.x.shape)
+    if solver == "vbd":
+        make = lambda: N.VbdSolver([obj], dt=1 / 120, iterations=20, gravity=scenes.GRAVITY)  # noqa: E731
+    else:
+        make = lambda: N.XpbdSolver([obj], dt=1 / 120, substeps=10, gravity=scenes.GRAVITY)  # noqa: E731
+    a, b = make(), make()
+    xp = torch.empty((nv, 3), dtype=torch.float64, pin_memory=True).numpy()
+    vp = torch.empty((nv, 3), dtype=torch.float64, pin_memory=True).numpy()
+    xp[:] = x
+    vp[:] = v
+    a.set_state(0, x, v)
+    b.set_state(0, xp, vp)
+    for _ in range(3):
+        a.step()
+        b.step()
+    xa, va = a.state(0)
+    xp.fill(np.nan)
+    vp.fill(np.nan)
+    b.get_state_into(0, xp, vp)
+    assert np.array_equal(xa, xp) and np.array_equal(va, vp)
