@@ -304,12 +304,26 @@ def other_configs(local, only=None) -> dict:
     if want("batch_512_patches_30it"):
         batch = S.patch_batch(512, 16, 128, seed=2024).objects
         nv = sum(o.nv for o in batch)
+        peak, peak_kind = _measured_peaks()
+        alg = sum(algorithmic_bytes_per_iteration(o) for o in batch)
+
+        def roofline(ms_step):
+            achieved = alg * 30 / (ms_step * 1e-3) / 1e9
+            return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "peak_source": peak_kind, "algorithmic_bytes_per_sweep": alg}
+
         s = N.VbdSolver(batch, dt=1 / 60, iterations=30, gravity=GRAVITY, device=local)
         ms = statistics.mean(_timed_steps(s, 5))
-        out["batch_512_patches_30it"] = {"vertex_solves_per_s": nv * 30 / (ms * 1e-3), "ms_per_step": ms,
-                                         "vertices": nv, "colors": int(s.n_colors(-1)), "launch": list(s.launch()),
-                                         "graph": True}
+        entry = {"vertex_solves_per_s": nv * 30 / (ms * 1e-3), "ms_per_step": ms, "vertices": nv,
+                 "colors": int(s.n_colors(-1)), "launch": list(s.launch()), "graph": True, "roofline": roofline(ms)}
         s.close()
+        # The dataflow kernel on the same batch, beside the autotuner's pick.
+        s = N.VbdSolver(batch, dt=1 / 60, iterations=30, gravity=GRAVITY, device=local, kernel=3)
+        ms3 = statistics.mean(_timed_steps(s, 5))
+        entry["dataflow_kernel"] = {"vertex_solves_per_s": nv * 30 / (ms3 * 1e-3), "ms_per_step": ms3,
+                                    "launch": list(s.launch()), "roofline": roofline(ms3)}
+        s.close()
+        out["batch_512_patches_30it"] = entry
     if want("implicit_euler_cloth_33x33"):
         imp = N.ImplicitSolver([cloth], dt=1 / 60, substeps=1, gravity=GRAVITY, device=local)
         stats = [imp.step() for _ in range(8)][3:]

@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(kXpbdChunk) xpbd_flow_kernel(const DevTables T
 
 // ---------------------------------------------------------------------------------------
 // Synchronised XPBD: every substep of a step in one persistent cooperative launch, one CTA
-// per SM, with a counting grid barrier (about 1.5 us) after the prediction and after every
+// per SM, with a counting grid barrier after the prediction and after every
 // projection phase instead of a kernel boundary (about 6 us per graph node on the 513^2
 // cloth, whose substep has 28 phases). The phases, their work items and the per-item
 // arithmetic are those of the phase launches (with L2-coherent loads), so the result is the
@@ -478,20 +478,41 @@ __global__ void __launch_bounds__(kXpbdSyncThreads) xpbd_sync_kernel(const DevTa
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     const float invh2 = 1.f / (h * h), invh = 1.f / h;
     int gen = 0;
+    // Each CTA takes an equal contiguous share of a phase's items (all SMs work on every
+    // phase); a thread's first item of the next phase, and the phase's table entry, are read
+    // before the barrier that precedes it (the tables are read-only), so that after the barrier
+    // only the element record and the positions remain on the dependency chain.
+    auto share = [&](const int4 &ph, int &first, int &end) {
+        const int per = (ph.y + int(gridDim.x) - 1) / int(gridDim.x);
+        first = min(ph.y, int(blockIdx.x) * per);
+        end = min(ph.y, first + per);
+    };
+    auto first_item = [&](const int4 &ph) {
+        int f, e;
+        share(ph, f, e);
+        return f + int(threadIdx.x) < e ? __ldg(items + ph.x + f + threadIdx.x) : -1;
+    };
     for (int s = 0; s < substeps; ++s) {
         for (int i = g; i < nv; i += TT) {
             if (s > 0) xpbd_velocity_vertex(pos, dold, vel, i, invh);
             xpbd_predict_vertex(pos, tgt, dold, vel, i, h, gx, gy, gz);
         }
+        int4 ph = Y.n_phases > 0 ? __ldg(Y.phase) : make_int4(0, 0, 0, 0);
+        int item = first_item(ph);
         if (!grid_counter_sync(Y.arrive, Y.status, gen, kXpbdMaxPolls, kXpbdSyncTimeout)) return;
         for (int p = 0; p < Y.n_phases; ++p) {
-            const int4 ph = __ldg(Y.phase + p);
-            for (int t = g; t < ph.y; t += TT) {
-                const int item = __ldg(items + ph.x + t);
+            int f, e;
+            share(ph, f, e);
+            for (int t = f + threadIdx.x; t < e; t += blockDim.x) {
+                const int it = t == f + int(threadIdx.x) ? item : __ldg(items + ph.x + t);
                 if (ph.z)
-                    project_anchor<true>(T, anchor_v, pos, invm, item, invh2);
+                    project_anchor<true>(T, anchor_v, pos, invm, it, invh2);
                 else
-                    project_item<kPaths, true>(T, pos, invm, item, invh2);
+                    project_item<kPaths, true>(T, pos, invm, it, invh2);
+            }
+            if (p + 1 < Y.n_phases) {
+                ph = __ldg(Y.phase + p + 1);
+                item = first_item(ph);
             }
             if (!grid_counter_sync(Y.arrive, Y.status, gen, kXpbdMaxPolls, kXpbdSyncTimeout)) return;
         }
