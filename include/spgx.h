@@ -359,14 +359,16 @@ spgx_status spgx_eval_vertex_blocks(int32_t type, int32_t n, const double *X, co
  * that leaves nothing to cudaMalloc), or code paths that must not add allocation latency
  * or fragmentation after start-up. It calls no cudaMalloc, cudaFree or other allocating
  * routine: inputs and outputs are the caller's host arrays, and the device staging is one
- * fixed array inside the library (about 750 KB, held by every GPU that loads the library
- * until the process exits). Capacity: n <= 4096 incidences per call; larger n returns
+ * fixed array inside the library (about 750 KB on each GPU it was called on, until the
+ * process exits). Capacity: n <= 4096 incidences per call; larger n returns
  * SPGX_ERR_INVALID_ARG (so do types with more than 4 stencil vertices or 22 parameters; all
  * fourteen fit). The first call on a device loads the library's device code there, which
- * places the array: make it at start-up, before another allocator takes the device's memory,
- * and before any stream capture. Every call looks up the array's device address (no
- * allocation). All calls share the array: calls that overlap on the same GPU race. Results
- * equal spgx_eval_vertex_blocks'. No counterpart in the reference. */
+ * places the array: make it at start-up, before another allocator takes the device's memory.
+ * Every call looks up the array's device address (no allocation). The function is never
+ * capture-safe: it copies synchronously and launches on the legacy default stream, so it must
+ * not be called while any stream of the process is being captured. All calls share the
+ * array: calls that overlap on the same GPU race. Results equal spgx_eval_vertex_blocks'. No
+ * counterpart in the reference. */
 spgx_status spgx_eval_vertex_blocks_noalloc(int32_t type, int32_t n, const double *X, const double *params,
                                             const int32_t *slots, double *grad, double *hess);
 /* Constraint values (n * nc) and gradients (n * nc * 3 * stencil_size, constraint-major)
