@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kTileThreads) vbd_tile_kernel(const TileView V
 // takes its next ticket while it polls for the current one: the smallest unfinished ticket is
 // then always running (a CTA holding it unstarted would be running a smaller unfinished one),
 // so progress is kept.
-constexpr int kFlowMaxPolls = 1 << 21;  // with 128 ns sleeps and an L2 round trip: about a second per wait
+constexpr int kFlowMaxPolls = 1 << 21;  // each poll an L2 round trip (a few hundred ns): about a second per wait
 constexpr int kFlowPollMax = 64;       // neighbour-list entries prefetched per task (the rest are read directly)
 
 template <int G, bool kGeneric>
@@ -298,7 +298,8 @@ __global__ void __launch_bounds__(kTileThreads) vbd_flow_kernel(const TileView V
                         ok = false;
                         break;
                     }
-                    __nanosleep(128);
+                    // No sleep between polls: a dependency is seen one L2 round trip after its
+                    // release (a 128 ns sleep cost 1.3 % of the step on the 513^2 cloth).
                 }
             }
             ok = __all_sync(0xffffffffu, ok);
