@@ -298,19 +298,27 @@ __device__ __forceinline__ void project_anchor(const DevTables &T, const int *__
     project_block<1, 1, kCoh>(pos, idx, w, C, g, cmp, invh2);
 }
 
+// Work item t of a phase: item0 + t when the phase covers consecutive elements of one type
+// (item0 >= 0), else the phase's item list.
+__device__ __forceinline__ int phase_item(const int *__restrict__ items, int item0, int t)
+{
+    return item0 >= 0 ? item0 + t : __ldg(items + t);
+}
+
 template <int kPaths>
 __global__ void __launch_bounds__(256) xpbd_phase_kernel(const DevTables T, float4 *pos, const float *__restrict__ invm,
-                                                         const int *__restrict__ items, int n, float invh2)
+                                                         const int *__restrict__ items, int item0, int n, float invh2)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) project_item<kPaths, false>(T, pos, invm, __ldg(items + t), invh2);
+    if (t < n) project_item<kPaths, false>(T, pos, invm, phase_item(items, item0, t), invh2);
 }
 
 __global__ void xpbd_anchor_kernel(const DevTables T, const int *__restrict__ anchor_v, float4 *pos,
-                                   const float *__restrict__ invm, const int *__restrict__ items, int n, float invh2)
+                                   const float *__restrict__ invm, const int *__restrict__ items, int item0, int n,
+                                   float invh2)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) project_anchor<false>(T, anchor_v, pos, invm, __ldg(items + t), invh2);
+    if (t < n) project_anchor<false>(T, anchor_v, pos, invm, phase_item(items, item0, t), invh2);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -459,7 +467,7 @@ constexpr int kXpbdSyncThreads = 512;
 constexpr int kXpbdSyncTimeout = 1;
 
 struct XpbdSyncView {
-    const int4 *phase;  // per phase: {first item, items, anchors, 0}
+    const int4 *phase;  // per phase: {first item, items, anchors, item0 (phase_item)}
     int n_phases;
     int *arrive;        // the grid barrier's counter (zeroed before each launch)
     int *status;        // kXpbdSyncTimeout when a barrier wait gave up
@@ -490,7 +498,7 @@ __global__ void __launch_bounds__(kXpbdSyncThreads) xpbd_sync_kernel(const DevTa
     auto first_item = [&](const int4 &ph) {
         int f, e;
         share(ph, f, e);
-        return f + int(threadIdx.x) < e ? __ldg(items + ph.x + f + threadIdx.x) : -1;
+        return f + int(threadIdx.x) < e ? phase_item(items + ph.x, ph.w, f + threadIdx.x) : -1;
     };
     for (int s = 0; s < substeps; ++s) {
         for (int i = g; i < nv; i += TT) {
@@ -504,7 +512,7 @@ __global__ void __launch_bounds__(kXpbdSyncThreads) xpbd_sync_kernel(const DevTa
             int f, e;
             share(ph, f, e);
             for (int t = f + threadIdx.x; t < e; t += blockDim.x) {
-                const int it = t == f + int(threadIdx.x) ? item : __ldg(items + ph.x + t);
+                const int it = t == f + int(threadIdx.x) ? item : phase_item(items + ph.x, ph.w, t);
                 if (ph.z)
                     project_anchor<true>(T, anchor_v, pos, invm, it, invh2);
                 else
@@ -524,6 +532,7 @@ struct XpbdPhase {
     int offset;
     int count;
     bool anchors;
+    int item0;  // the first item when the phase's items are consecutive elements of one type, else -1
 };
 
 struct XpbdSolver {
@@ -599,9 +608,6 @@ struct XpbdSolver {
         SPGX_CUDA(cudaEventCreate(&ev0));
         SPGX_CUDA(cudaEventCreate(&ev1));
         SPGX_TRY_STATUS(X.init(L));
-        SPGX_TRY_STATUS(EB.upload(L.el, T));
-        SPGX_TRY_STATUS(EB.upload_generic(L, T));
-        SPGX_TRY_STATUS(d_anchor_v.upload(L.el.anchor_v));
         const size_t cap = size_t(1) << kItemShift;
         if (L.el.anchors.size() >= cap || L.el.springs.size() >= cap || L.el.bend_idx.size() >= cap ||
             L.el.stvk_idx.size() >= cap || L.el.snh_idx.size() >= cap || L.el.gen_idx.size() >= cap) {
@@ -620,7 +626,7 @@ struct XpbdSolver {
                     for (int c : O.stencil_colors[k]) max_c = std::max(max_c, c + 1);
             for (int c = 0; c < max_c; ++c) {
                 for (int anch = 0; anch < 2; ++anch) {
-                    XpbdPhase ph{static_cast<int>(items.size()), 0, anch == 1};
+                    XpbdPhase ph{static_cast<int>(items.size()), 0, anch == 1, -1};
                     for (size_t o = 0; o < L.objects.size(); ++o) {
                         const auto &O = L.objects[o];
                         if (k >= static_cast<int>(O.stencil_colors.size())) continue;
@@ -637,6 +643,16 @@ struct XpbdSolver {
                 }
             }
         }
+        renumber_in_phase_order(items);
+        SPGX_TRY_STATUS(EB.upload(el, T));
+        SPGX_TRY_STATUS(EB.upload_generic(L, T));
+        if (!el.gen_idx.empty()) {  // this handle's order of the generic elements (parameters stay put)
+            SPGX_TRY_STATUS(EB.gen_idx.upload(el.gen_idx));
+            SPGX_TRY_STATUS(EB.gen_info.upload(el.gen_info));
+            T.gen_idx = EB.gen_idx.as<int4>();
+            T.gen_info = EB.gen_info.as<int4>();
+        }
+        SPGX_TRY_STATUS(d_anchor_v.upload(el.anchor_v));
         SPGX_TRY_STATUS(d_items.upload(items));
         items_host = items;
         SPGX_TRY_STATUS(setup_paths());
@@ -647,7 +663,7 @@ struct XpbdSolver {
     spgx_status setup_sync()
     {
         std::vector<I4> tab;
-        for (const auto &ph : phases) tab.push_back(I4{ph.offset, ph.count, ph.anchors ? 1 : 0, 0});
+        for (const auto &ph : phases) tab.push_back(I4{ph.offset, ph.count, ph.anchors ? 1 : 0, ph.item0});
         if (tab.empty()) tab.push_back(I4{0, 0, 0, 0});
         SPGX_TRY_STATUS(sy_phase.upload(tab));
         SPGX_TRY_STATUS(sy_sync.alloc(2 * sizeof(int)));
@@ -708,12 +724,72 @@ struct XpbdSolver {
         return SPGX_OK;
     }
 
-    // Vertices of one work item (internal indices).
+    // This handle's element tables: each energy type's elements renumbered in the order the
+    // phases visit them, so that a phase of one type covers consecutive elements. Its kernels
+    // then take element first + t without reading a work-item list, and its record loads are
+    // coalesced. The projections and their order per vertex are unchanged.
+    ElementTables el;
+
+    void renumber_in_phase_order(std::vector<int32_t> &items)
+    {
+        const ElementTables &E = L.el;
+        el = E;
+        std::vector<int32_t> next(8, 0);
+        for (auto &it : items) {
+            const int type = (it >> kItemShift) & 7;
+            const int e = it & kItemMask;
+            const int n = next[type]++;
+            switch (type) {
+            case SPGX_ENERGY_SPRING_ANCHOR:
+                el.anchors[n] = E.anchors[e];
+                el.anchor_v[n] = E.anchor_v[e];
+                el.anchor_cmp[n] = E.anchor_cmp[e];
+                break;
+            case SPGX_ENERGY_SPRING:
+                el.springs[n] = E.springs[e];
+                el.spring_cmp[n] = E.spring_cmp[e];
+                break;
+            case SPGX_ENERGY_DISCRETE_BENDING:
+                el.bend_idx[n] = E.bend_idx[e];
+                el.bend_prm[n] = E.bend_prm[e];
+                break;
+            case SPGX_ENERGY_MEMBRANE_STVK:
+                el.stvk_idx[n] = E.stvk_idx[e];
+                el.stvk_D[n] = E.stvk_D[e];
+                el.stvk_Ka[n] = E.stvk_Ka[e];
+                el.stvk_Kb[n] = E.stvk_Kb[e];
+                el.stvk_Ca[n] = E.stvk_Ca[e];
+                el.stvk_Cb[n] = E.stvk_Cb[e];
+                el.stvk_Cc[n] = E.stvk_Cc[e];
+                break;
+            case kItemGeneric:
+                el.gen_idx[n] = E.gen_idx[e];
+                el.gen_info[n] = E.gen_info[e];
+                break;
+            default:
+                el.snh_idx[n] = E.snh_idx[e];
+                el.snh_p0[n] = E.snh_p0[e];
+                el.snh_p1[n] = E.snh_p1[e];
+                el.snh_p2[n] = E.snh_p2[e];
+                el.snh_cmp[n] = E.snh_cmp[e];
+                break;
+            }
+            it = (type << kItemShift) | n;
+        }
+        // A phase whose items are one type's consecutive elements runs without its item list.
+        for (auto &ph : phases) {
+            ph.item0 = items[ph.offset];
+            for (int t = 1; t < ph.count && ph.item0 >= 0; ++t)
+                if (items[ph.offset + t] != ph.item0 + t) ph.item0 = -1;
+        }
+    }
+
+    // Vertices of one work item (internal indices, this handle's element order).
     int item_vertices(int item, int *v) const
     {
         const int type = (item >> kItemShift) & 7;
         const int e = item & kItemMask;
-        const ElementTables &E = L.el;
+        const ElementTables &E = el;
         switch (type) {
         case SPGX_ENERGY_SPRING_ANCHOR: v[0] = E.anchor_v[e]; return 1;
         case SPGX_ENERGY_SPRING: v[0] = E.springs[e].x, v[1] = E.springs[e].y; return 2;
@@ -883,17 +959,17 @@ struct XpbdSolver {
         return SPGX_OK;
     }
 
-    void launch_phase(int grid, cudaStream_t st, const int *items, int n, float invh2)
+    void launch_phase(int grid, cudaStream_t st, const int *items, int item0, int n, float invh2)
     {
         switch (paths) {
-        case 0: xpbd_phase_kernel<0><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        case 1: xpbd_phase_kernel<1><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        case 2: xpbd_phase_kernel<2><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        case 3: xpbd_phase_kernel<3><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        case 4: xpbd_phase_kernel<4><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        case 5: xpbd_phase_kernel<5><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        case 6: xpbd_phase_kernel<6><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
-        default: xpbd_phase_kernel<7><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, n, invh2); break;
+        case 0: xpbd_phase_kernel<0><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        case 1: xpbd_phase_kernel<1><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        case 2: xpbd_phase_kernel<2><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        case 3: xpbd_phase_kernel<3><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        case 4: xpbd_phase_kernel<4><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        case 5: xpbd_phase_kernel<5><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        case 6: xpbd_phase_kernel<6><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
+        default: xpbd_phase_kernel<7><<<grid, block, 0, st>>>(T, X.pos(), X.invm(), items, item0, n, invh2); break;
         }
     }
 
@@ -904,9 +980,9 @@ struct XpbdSolver {
             const int grid = (ph.count + block - 1) / block;
             if (ph.anchors)
                 xpbd_anchor_kernel<<<grid, block, 0, st>>>(T, d_anchor_v.as<int>(), X.pos(), X.invm(),
-                                                           d_items.as<int>() + ph.offset, ph.count, invh2);
+                                                           d_items.as<int>() + ph.offset, ph.item0, ph.count, invh2);
             else
-                launch_phase(grid, st, d_items.as<int>() + ph.offset, ph.count, invh2);
+                launch_phase(grid, st, d_items.as<int>() + ph.offset, ph.item0, ph.count, invh2);
         }
     }
 
