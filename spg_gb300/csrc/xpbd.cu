@@ -386,6 +386,17 @@ __device__ __forceinline__ void xpbd_velocity_vertex(const float4 *pos, const fl
     vel[i] = make_float4((d.x - o.x) * invh, (d.y - o.y) * invh, (d.z - o.z) * invh, 0.f);
 }
 
+// Between two substeps of the phase launches: the velocity update of the one that ended and the
+// inertial prediction of the next, in one pass (each touches one vertex only).
+__global__ void xpbd_between_substeps_kernel(float4 *pos, float4 *tgt, float4 *dold, float4 *vel, int nv, float invh,
+                                             float h, float gx, float gy, float gz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    xpbd_velocity_vertex(pos, dold, vel, i, invh);
+    xpbd_predict_vertex(pos, tgt, dold, vel, i, h, gx, gy, gz);
+}
+
 template <int kPaths>
 __global__ void __launch_bounds__(kXpbdChunk) xpbd_flow_kernel(const DevTables T, float4 *pos, float4 *tgt,
                                                                float4 *dold, float4 *vel,
@@ -393,12 +404,11 @@ __global__ void __launch_bounds__(kXpbdChunk) xpbd_flow_kernel(const DevTables T
                                                                const int *__restrict__ items,
                                                                const int *__restrict__ anchor_v,
                                                                const XpbdFlowView F, int n_chunks, int substeps,
-                                                               int epoch_base, float h, float gx, float gy, float gz,
-                                                               unsigned int *status)
+                                                               int epoch_base, float h, float invh, float invh2,
+                                                               float gx, float gy, float gz, unsigned int *status)
 {
     __shared__ int s_task, s_fail;
     const int total = substeps * n_chunks;
-    const float invh2 = 1.f / (h * h), invh = 1.f / h;
     for (;;) {
         if (threadIdx.x == 0) s_task = ld_relaxed_gpu(F.ticket + 1) ? total : atomicAdd(F.ticket, 1);
         __syncthreads();
@@ -480,11 +490,11 @@ __global__ void __launch_bounds__(kXpbdSyncThreads) xpbd_sync_kernel(const DevTa
                                                                      const int *__restrict__ items,
                                                                      const int *__restrict__ anchor_v,
                                                                      const XpbdSyncView Y, int nv, int substeps,
-                                                                     float h, float gx, float gy, float gz)
+                                                                     float h, float invh, float invh2, float gx,
+                                                                     float gy, float gz)
 {
     const int TT = gridDim.x * blockDim.x;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    const float invh2 = 1.f / (h * h), invh = 1.f / h;
     int gen = 0;
     // Each CTA takes an equal contiguous share of a phase's items (all SMs work on every
     // phase); a thread's first item of the next phase, and the phase's table entry, are read
@@ -719,7 +729,8 @@ struct XpbdSolver {
         const int *items = d_items.as<int>(), *av = d_anchor_v.as<int>();
         XpbdSyncView Y{sy_phase.as<int4>(), static_cast<int>(phases.size()), sy_sync.as<int>(), sy_sync.as<int>() + 1};
         int nv = L.nv, ns = P.substeps;
-        void *args[] = {&Tt, &pos, &tgt, &dold, &vel, &invm, &items, &av, &Y, &nv, &ns, &h, &gx, &gy, &gz};
+        float invh = static_cast<float>(1.0 / h_sub), invh2 = static_cast<float>(1.0 / (h_sub * h_sub));
+        void *args[] = {&Tt, &pos, &tgt, &dold, &vel, &invm, &items, &av, &Y, &nv, &ns, &h, &invh, &invh2, &gx, &gy, &gz};
         SPGX_CUDA(cudaLaunchKernelExC(&cfg, sync_fn(), args));
         return SPGX_OK;
     }
@@ -944,8 +955,9 @@ struct XpbdSolver {
         const int *items = d_items.as<int>(), *av = d_anchor_v.as<int>();
         unsigned int *status = d_status.as<unsigned int>();
         int nc = n_chunks, ns = P.substeps, base = flow_epoch;
-        void *args[] = {&Tt, &pos, &tgt, &dold, &vel, &invm, &items, &av, &FV, &nc, &ns, &base, &h, &gx, &gy, &gz,
-                        &status};
+        float invh = static_cast<float>(1.0 / h_sub), invh2 = static_cast<float>(1.0 / (h_sub * h_sub));
+        void *args[] = {&Tt, &pos, &tgt, &dold, &vel, &invm, &items, &av, &FV, &nc, &ns, &base, &h, &invh, &invh2,
+                        &gx, &gy, &gz, &status};
         SPGX_CUDA(cudaLaunchKernelExC(&cfg, flow_fn(), args));
         flow_epoch += P.substeps;
         return SPGX_OK;
@@ -988,11 +1000,16 @@ struct XpbdSolver {
 
     void launch_step(cudaStream_t st)
     {
+        launch_begin_substep(X, h_sub, P.gravity, st);
         for (int s = 0; s < P.substeps; ++s) {
-            launch_begin_substep(X, h_sub, P.gravity, st);
             launch_phases(st);
-            launch_end_substep(X, h_sub, st);
+            if (s + 1 < P.substeps && L.nv > 0)
+                xpbd_between_substeps_kernel<<<(L.nv + 255) / 256, 256, 0, st>>>(
+                    X.pos(), X.tgt(), X.dold(), X.vel(), L.nv, static_cast<float>(1.0 / h_sub), static_cast<float>(h_sub),
+                    static_cast<float>(P.gravity[0]), static_cast<float>(P.gravity[1]),
+                    static_cast<float>(P.gravity[2]));
         }
+        launch_end_substep(X, h_sub, st);
     }
 
     spgx_status build_graph()
