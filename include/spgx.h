@@ -179,7 +179,9 @@ typedef struct spgx_vbd_params {
     double gravity[3];         /* BaseSolver::setGravity (baseSolver.h:32) */
     double tolerance;          /* > 0: iterate until ||r|| <= tolerance * ||r(y)||, see below */
     int32_t max_iterations;    /* cap per substep when tolerance > 0 */
-    int32_t check_interval;    /* iterations between residual checks when tolerance > 0 */
+    int32_t check_interval;    /* iterations between residual checks when tolerance > 0; once two
+                                * checks give a decay rate, the last interval is cut to the
+                                * iterations that rate needs (5 % margin, at least 10) */
     double fallback_condition; /* 3x3 blocks whose condition estimate exceeds this are solved in FP64 */
     int32_t lanes_per_vertex;  /* 0 = autotune; else 1, 2, 4, 8, 16 or 32 */
     int32_t block_size;        /* 0 = autotune; else a multiple of 32 up to 256 (lanes kernel) */

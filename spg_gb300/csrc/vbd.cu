@@ -1310,9 +1310,23 @@ spgx_status VbdSolver::step(spgx_step_stats *stats, float *features, float *targ
             // computed them already.
             if (record && W.mode != kWarmLearned) launch_warm_features(W, X.vel(), L.nv, h_sub, P.gravity, stream);
             if (P.tolerance > 0) {
-                int it = probe;
+                // Sweeps run in chunks of check_interval between residual checks. Once two
+                // checks give a decay rate, the next chunk is cut to the sweeps that rate needs to
+                // reach the tolerance (5 % margin, at least kMinCheckChunk): a check costs about
+                // one sweep, and a full last chunk would overshoot by half an interval on average.
+                constexpr int kMinCheckChunk = 10;
+                int it = probe, it_prev = -1;
+                double r_prev = 0.0;
                 while (it < P.max_iterations && r > P.tolerance * r0) {
-                    const int chunk = std::min(P.check_interval, P.max_iterations - it);
+                    int chunk = std::min(P.check_interval, P.max_iterations - it);
+                    if (it_prev >= 0 && r < r_prev && r > 0.0) {
+                        const double rate = std::log(r / r_prev) / double(it - it_prev);  // per sweep, < 0
+                        const double need = std::log(P.tolerance * r0 / r) / rate;
+                        if (std::isfinite(need) && need > 0.0)
+                            chunk = std::min(chunk, std::max(kMinCheckChunk, static_cast<int>(std::ceil(1.05 * need))));
+                    }
+                    r_prev = r;
+                    it_prev = it;
                     launch_iterations(*this, chunk, stream);
                     it += chunk;
                     SPGX_TRY_STATUS(residual_norm(&r));
