@@ -325,7 +325,7 @@ spgx_status spgx_mlp_train(spgx_mlp *h, int32_t n, const float *x, const float *
  * mode 1 the learned guess (mlp required); mode 2 the previous step's acceleration carried
  * over, x_e = x_n + 2 (x_n - x_{n-1}) - (x_{n-1} - x_{n-2}) (no network; a baseline for
  * the learned guess). Mode 2 keeps x_e only when its residual is below y's. Mode 1 forms
- * x_w = x_e + l * smoothed network correction, runs 20 sweeps from each of x_w and x_e, and
+ * x_w = x_e + l * smoothed network correction, runs 40 sweeps from each of x_w and x_e, and
  * continues from the one with the lower residual (the sweeps of the other one are spent and
  * counted in spgx_step_stats.iterations; residual_warm / residual_extrapolated are the
  * residuals after those sweeps).

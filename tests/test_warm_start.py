@@ -78,10 +78,11 @@ def test_extrapolated_guess_cuts_iterations_to_tolerance():
 
 @pytest.mark.gpu
 def test_learned_guess_with_the_shipped_network():
-    """The learned mode (extrapolation plus the shipped network's correction; 20 sweeps from
+    """The learned mode (extrapolation plus the shipped network's correction; 40 sweeps from
     each of the two guesses, then the lower residual continues) reaches the tolerance in at
     most 2/3 of the inertial guess's iterations, and never needs more than the extrapolated
-    guess alone by more than the check granularity (the counts include both probes)."""
+    guess alone plus the probes' sweeps (the counts include both probes). On this smooth 129^2
+    case the network adds nothing (measured: 320 against 150, the extrapolated guess kept)."""
     mlp = W.load_mlp()
     plain, _ = _iterations(0)
     learned, picks = _iterations(1, mlp)
@@ -89,7 +90,7 @@ def test_learned_guess_with_the_shipped_network():
     print(f"iterations to 1e-5 over 4 steps: inertial {plain}, extrapolated {extrap}, learned {learned} "
           f"(network's guess picked {picks[0]}x, extrapolated {picks[1]}x)")
     assert plain >= 1.5 * max(learned, 1)
-    assert learned <= extrap + 4 * 50
+    assert learned <= extrap + 4 * 2 * 40
 
 
 @pytest.mark.gpu
@@ -97,12 +98,12 @@ def test_learned_guess_with_the_shipped_network():
 def test_learned_guess_beats_the_extrapolated_guess_on_the_large_cloth():
     """The benchmark's protocol on the 513x513 cloth (fresh from rest, two untimed steps, then
     three steps solved to 1e-5, residual checked every 200 iterations): the learned mode, probes
-    included, needs at least 10 % fewer iterations than the extrapolated guess alone, and the
-    network's guess is the one kept in at least one of the steps."""
+    included, needs at most 0.6 of the extrapolated guess's iterations (measured 840 against
+    1,803), and the network's guess is the one kept in most of the steps (measured: all three)."""
     mlp = W.load_mlp()
     learned, picks = _iterations(1, mlp, n=513, steps=3, check=200)
     extrap, _ = _iterations(2, n=513, steps=3, check=200)
     print(f"513 cloth, iterations to 1e-5 over 3 steps: extrapolated {extrap}, learned {learned} "
           f"(network's guess kept {picks[0]}x)")
-    assert picks[0] >= 1
-    assert learned <= 0.9 * extrap
+    assert picks[0] >= 2
+    assert learned <= 0.6 * extrap
