@@ -830,7 +830,7 @@ struct ImplicitSolver {
     DevBuf d_wide;  // the matrix is out of double-float range
     // The double-float CG: symmetric matrix, vectors, block partials and barrier state.
     DevBuf d_urow, d_ucol, d_uval, d_ufull, d_lrow, d_lent;
-    DevBuf d_x2, d_r2, d_p2, d_Ap2, d_d2, d_part, d_sync;
+    DevBuf d_x2, d_r2, d_p2, d_Ap2, d_d2, d_u2, d_w2, d_part, d_sync;
     HostBuf h_dots, h_ctl, h_sync;
     CgSymDf SD{};
     int cg_lanes{4}, cg_blocks{0};
@@ -1023,7 +1023,7 @@ struct ImplicitSolver {
         for (DevBuf *b : {&d_x, &d_v, &d_x0, &d_v0, &d_vi, &d_xm1, &d_vm1, &d_f, &d_b, &d_u, &d_w, &d_dx, &d_r, &d_z,
                           &d_p, &d_Ap, &d_dinv})
             SPGX_TRY_STATUS(b->alloc(vb));
-        for (DevBuf *b : {&d_x2, &d_r2, &d_p2, &d_Ap2, &d_d2})
+        for (DevBuf *b : {&d_x2, &d_r2, &d_p2, &d_Ap2, &d_d2, &d_u2, &d_w2})
             SPGX_TRY_STATUS(b->alloc(size_t(std::max(1, nv)) * 2 * sizeof(float4)));
         SPGX_TRY_STATUS(d_wide.alloc(sizeof(int)));
         SPGX_TRY_STATUS(d_sync.alloc(sizeof(CgSync)));
@@ -1135,7 +1135,8 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaMemsetAsync(d_sync.as<void>(), 0, sizeof(CgSync), stream));
         SPGX_CUDA(cudaGetLastError());
         CgDfVecs V{vec(d_b), vec(d_dinv), vec(d_dx), d_x2.as<float4>(), d_r2.as<float4>(), d_p2.as<float4>(),
-                   d_Ap2.as<float4>(), d_d2.as<float4>(), d_part.as<double>(), n, nv};
+                   d_Ap2.as<float4>(), d_d2.as<float4>(), d_u2.as<float4>(), d_w2.as<float4>(), d_part.as<double>(), n,
+                   nv};
         CgSync *sync = d_sync.as<CgSync>();
         CgControl *ctl = d_ctl.as<CgControl>();
         const int *wide = T.wide;

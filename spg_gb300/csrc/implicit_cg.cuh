@@ -12,18 +12,18 @@
 //   j < i, as the transposes of the stored (j, i). The rows are in reverse Cuthill-McKee
 //   order, so block (j, i) was read by row j a few hundred rows earlier and is still in L2.
 // - One launch holds the whole solve, one block of 1024 threads per SM, each block owning an
-//   equal contiguous range of rows in every phase. Three grid barriers per iteration (after the
-//   product, after the update, after the direction). A barrier is a counter every block adds
-//   to (release) and polls (acquire) until all blocks have arrived; each block then sums every
-//   block's partials itself, in the same fixed order, so alpha, beta and the stopping decision
-//   are identical everywhere without a second round trip, and the solve is deterministic.
-//   Every wait is bounded; a wait that runs out sets a status the host reports.
+//   equal contiguous range of rows in every phase. Two grid barriers per iteration: after the
+//   product with its dot products (a reduction), and after the vector update. A barrier is a
+//   counter every block adds to (release) and polls (acquire) until all blocks have arrived;
+//   after a reduction each block sums every block's partials itself, in the same fixed order,
+//   so alpha, beta and the stopping decision are identical everywhere without a second round
+//   trip, and the solve is deterministic. Every wait is bounded; a wait that runs out sets a
+//   status the host reports.
 //
 // Stopping rule and iteration count are those of the FP64 path: |r|^2 < tol^2 |b|^2 after an
 // update, or max_its updates.
 
 constexpr int kCgThreads = 1024;
-constexpr int kCgRegRows = 2;         // rows a thread keeps z and p of in registers across the update barrier
 constexpr int kCgMaxPolls = 1 << 21;  // with 32 ns sleeps and an L2 round trip: about a second per wait
 
 // Symmetric block matrix in double-float: for row i the upper blocks (i, j), j >= i, diagonal
@@ -46,7 +46,8 @@ struct CgDfVecs {
     const double *b;     // right-hand side (FP64, 3 per row)
     const double *dinv;  // diagonal preconditioner 1 / A_ii (FP64, 3 per row)
     double *x;           // the solution, written in FP64 at the end
-    float4 *x2, *r2, *p2, *Ap2, *d2;
+    float4 *x2, *r2, *p2, *Ap2, *d2;  // Ap2 holds s = A p (kept by recurrence)
+    float4 *u2, *w2;                   // u = D^-1 r and w = A u
     double *part;        // per barrier parity and block: {p.Ap, r.r, r.z, out of range}
     int n, nv;
 };
@@ -216,41 +217,46 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
     __shared__ float2 s_scalar;  // alpha or beta in double-float, for the vector phases
     int gen = 0;
 
-    // Start (x = 0): r = b, z = D^-1 r, p = z.
+    // The iteration in the Chronopoulos-Gear form of preconditioned CG (the same iterates as
+    // Eigen's CG in exact arithmetic): with u = D^-1 r, w = A u, gamma = r.u, delta = u.w,
+    //   beta = gamma / gamma_prev, alpha = gamma / (delta - beta gamma / alpha_prev),
+    //   p = u + beta p, s = w + beta s (s = A p by recurrence), x += alpha p, r -= alpha s,
+    // so the product and all three dot products (with r.r for the stopping test) need one
+    // grid reduction per iteration instead of two. The stopping test (|r|^2 < tol^2 |b|^2 after
+    // an update, or max_its updates) and the iteration count are those of the FP64 path.
+
+    // Start (x = 0, p = s = 0): r = b, u = D^-1 r.
+    bool bad = false;
     {
-        float2 rr = make_float2(0.f, 0.f), rz = rr;
-        bool bad = false;
+        const DF3 zero3{{make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)}};
         for (int i = r0 + threadIdx.x; i < r1; i += kCgThreads) {
-            DF3 r, d, z;
+            DF3 r, d, u;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 bool o1, o2;
                 r.v[c] = split_df(V.b[3 * size_t(i) + c], o1);
                 d.v[c] = split_df(V.dinv[3 * size_t(i) + c], o2);
-                z.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
-                rr = df_madd(r.v[c], r.v[c], rr);
-                rz = df_madd(r.v[c], z.v[c], rz);
+                u.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
                 bad |= o1 | o2;
             }
-            st_row(V.x2, i, DF3{{make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)}});
+            st_row(V.x2, i, zero3);
             st_row(V.r2, i, r);
             st_row(V.d2, i, d);
-            st_row(V.p2, i, z);
+            st_row(V.u2, i, u);
+            st_row(V.p2, i, zero3);
+            st_row(V.Ap2, i, zero3);
         }
-        cg_allreduce(V, S, gen, make_float2(0.f, 0.f), rr, rz, bad, s_tot);
+        cg_grid_sync(S, gen);  // u complete before the product gathers it
     }
-    // Eigen's start: nothing to do for b = 0; otherwise iterate while |r|^2 >= thr2.
-    const double rr0 = s_tot[1];
-    const double thr2 = fmax(tol * tol * rr0, 1e-300);
-    double rz = s_tot[2], rr_last = rr0;
+    __shared__ double s_alpha;
+    double rr0 = 0.0, thr2 = 0.0, rr_last = 0.0, gamma_prev = 0.0, alpha_prev = 1.0;
     int its = 0;
-    bool out_of_range = s_tot[3] != 0.0;
-    bool done = out_of_range || rr0 == 0.0 || rr0 < thr2 || max_its <= 0;
+    bool out_of_range = false;
 
-    while (!done && !cg_status(S)) {
-        // Ap = A p (upper blocks, then the transposes of the lower ones), p . Ap.
+    for (int k = 0; !cg_status(S); ++k) {
+        // w = A u (upper blocks, then the transposes of the lower ones); r.u, r.r, u.w.
         {
-            float2 pap = make_float2(0.f, 0.f);
+            float2 ru = make_float2(0.f, 0.f), rr = ru, uw = ru;
             const int w = threadIdx.x >> 5, lane = threadIdx.x & (LANES - 1);
             for (int base = r0 + w * (32 / LANES); base < r1; base += kCgThreads / LANES) {
                 const int i = base + (threadIdx.x & 31) / LANES;
@@ -258,20 +264,20 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
                 if (i < r1) {
                     const int u0 = __ldg(A.urow + i), nu = __ldg(A.urow + i + 1) - u0;
                     const int w0 = __ldg(A.lrow + i), nl = __ldg(A.lrow + i + 1) - w0;
-                    // Upper blocks: row r of block (i, c) times p_c. The next trip's column is
+                    // Upper blocks: row r of block (i, c) times u_c. The next trip's column is
                     // fetched before this trip's values are used.
                     int cn = lane < nu ? __ldg(A.ucol + u0 + lane) : 0;
                     for (int t = lane; t < nu; t += LANES) {
-                        const int k = u0 + t, c = cn;
-                        if (t + LANES < nu) cn = __ldg(A.ucol + k + LANES);
-                        cg_block_product<false>(A.ublk + kCgBlockFloat4 * size_t(k), ld_row(V.p2, c), h, l);
+                        const int kk = u0 + t, c = cn;
+                        if (t + LANES < nu) cn = __ldg(A.ucol + kk + LANES);
+                        cg_block_product<false>(A.ublk + kCgBlockFloat4 * size_t(kk), ld_row(V.u2, c), h, l);
                     }
                     // Lower blocks: block (i, c) is the transpose of the stored (c, i).
                     int2 en = lane < nl ? __ldg(A.lent + w0 + lane) : make_int2(0, 0);
                     for (int t = lane; t < nl; t += LANES) {
                         const int2 e = en;
                         if (t + LANES < nl) en = __ldg(A.lent + w0 + t + LANES);
-                        cg_block_product<true>(A.ublk + kCgBlockFloat4 * size_t(e.y), ld_row(V.p2, e.x), h, l);
+                        cg_block_product<true>(A.ublk + kCgBlockFloat4 * size_t(e.y), ld_row(V.u2, e.x), h, l);
                     }
                 }
 #pragma unroll
@@ -280,104 +286,80 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
                     for (int r = 0; r < 3; ++r)
                         df_add(h[r], l[r], __shfl_xor_sync(0xffffffffu, h[r], o), __shfl_xor_sync(0xffffffffu, l[r], o));
                 if (i < r1 && lane == 0) {
-                    const DF3 ap{{df_norm(h[0], l[0]), df_norm(h[1], l[1]), df_norm(h[2], l[2])}};
-                    st_row(V.Ap2, i, ap);
-                    const DF3 pi = ld_row(V.p2, i);
+                    const DF3 wi{{df_norm(h[0], l[0]), df_norm(h[1], l[1]), df_norm(h[2], l[2])}};
+                    st_row(V.w2, i, wi);
+                    const DF3 ri = ld_row(V.r2, i), ui = ld_row(V.u2, i);
 #pragma unroll
-                    for (int r = 0; r < 3; ++r) pap = df_madd(pi.v[r], ap.v[r], pap);
+                    for (int r = 0; r < 3; ++r) {
+                        ru = df_madd(ri.v[r], ui.v[r], ru);
+                        rr = df_madd(ri.v[r], ri.v[r], rr);
+                        uw = df_madd(ui.v[r], wi.v[r], uw);
+                    }
+                    bad |= df3_out_of_range(wi);
                 }
             }
-            cg_allreduce(V, S, gen, pap, make_float2(0.f, 0.f), make_float2(0.f, 0.f), false, s_tot);
+            cg_allreduce(V, S, gen, ru, rr, uw, bad, s_tot);
         }
         if (cg_status(S)) break;
-        if (threadIdx.x == 0) {
-            bool o;
-            s_scalar = split_df(rz / s_tot[0], o);
-        }
-        __syncthreads();
-
-        // x += alpha p; r -= alpha Ap; z = D^-1 r; r.r and r.z. The first kCgRegRows rows of
-        // each thread keep z and p in registers for the direction.
-        DF3 zr[kCgRegRows], pr[kCgRegRows];
-        {
-            const float2 alpha = s_scalar;
-            const float2 nalpha = df_neg(alpha);
-            float2 rr = make_float2(0.f, 0.f), rzp = rr;
-            bool bad = df_out_of_range(alpha);
-            float4 *__restrict__ xv = V.x2, *__restrict__ rv = V.r2;
-            const float4 *__restrict__ pv = V.p2, *__restrict__ av = V.Ap2, *__restrict__ dv = V.d2;
-            auto update = [&](int i, DF3 &z, DF3 &p) {
-                p = ld_row(pv, i);
-                DF3 x = ld_row(xv, i), r = ld_row(rv, i);
-                const DF3 ap = ld_row(av, i), d = ld_row(dv, i);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    x.v[c] = df_madd(alpha, p.v[c], x.v[c]);
-                    r.v[c] = df_madd(nalpha, ap.v[c], r.v[c]);
-                    z.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
-                    rr = df_madd(r.v[c], r.v[c], rr);
-                    rzp = df_madd(r.v[c], z.v[c], rzp);
-                }
-                st_row(xv, i, x);
-                st_row(rv, i, r);
-                bad |= df3_out_of_range(r);
-            };
-#pragma unroll
-            for (int j = 0; j < kCgRegRows; ++j)
-                if (r0 + threadIdx.x + j * kCgThreads < r1) update(r0 + threadIdx.x + j * kCgThreads, zr[j], pr[j]);
-            for (int i = r0 + threadIdx.x + kCgRegRows * kCgThreads; i < r1; i += kCgThreads) {
-                DF3 z, p;
-                update(i, z, p);
-            }
-            cg_allreduce(V, S, gen, make_float2(0.f, 0.f), rr, rzp, bad, s_tot);
-        }
-        if (cg_status(S)) break;
-        ++its;
+        const double gamma = s_tot[0], rr = s_tot[1], delta = s_tot[2];
         if (s_tot[3] != 0.0) {
             out_of_range = true;
             break;
         }
-        if (s_tot[1] < thr2 || its >= max_its) {
-            rr_last = s_tot[1];
-            break;
+        if (k == 0) {
+            // Eigen's start: nothing to do for b = 0; otherwise iterate while |r|^2 >= thr2.
+            rr0 = rr_last = rr;
+            thr2 = fmax(tol * tol * rr0, 1e-300);
+            if (rr0 == 0.0 || rr0 < thr2 || max_its <= 0) break;
+        } else {
+            ++its;
+            if (rr < thr2 || its >= max_its) {
+                rr_last = rr;
+                break;
+            }
         }
         if (threadIdx.x == 0) {
             bool o;
-            s_scalar = split_df(s_tot[2] / rz, o);
+            const double beta = k == 0 ? 0.0 : gamma / gamma_prev;
+            const double alpha = gamma / (delta - beta * gamma / alpha_prev);
+            s_scalar = split_df(beta, o);
+            s_alpha = alpha;
         }
-        rz = s_tot[2];
         __syncthreads();
+        const double alpha_d = s_alpha;
+        const float2 beta = s_scalar;
+        alpha_prev = alpha_d;
+        gamma_prev = gamma;
 
-        // p = z + beta p. The range check of p is reported with the next product's sums.
+        // p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = D^-1 r.
         {
-            const float2 beta = s_scalar;
-            bool bad = df_out_of_range(beta);
-            auto direction = [&](int i, const DF3 &z, const DF3 &p) {
-                DF3 q;
+            bool o;
+            const float2 alpha = split_df(alpha_d, o);
+            const float2 nalpha = df_neg(alpha);
+            bad = o || df_out_of_range(beta);
+            float4 *__restrict__ xv = V.x2, *__restrict__ rv = V.r2, *__restrict__ pv = V.p2,
+                                 *__restrict__ sv = V.Ap2, *__restrict__ uv = V.u2;
+            const float4 *__restrict__ wv = V.w2, *__restrict__ dv = V.d2;
+            for (int i = r0 + threadIdx.x; i < r1; i += kCgThreads) {
+                DF3 p = ld_row(pv, i), sr = ld_row(sv, i), x = ld_row(xv, i), r = ld_row(rv, i);
+                const DF3 u = ld_row(uv, i), wi = ld_row(wv, i), d = ld_row(dv, i);
+                DF3 un;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) q.v[c] = df_madd(beta, p.v[c], z.v[c]);
-                st_row(V.p2, i, q);
-                bad |= df3_out_of_range(q);
-            };
-#pragma unroll
-            for (int j = 0; j < kCgRegRows; ++j)
-                if (r0 + threadIdx.x + j * kCgThreads < r1) direction(r0 + threadIdx.x + j * kCgThreads, zr[j], pr[j]);
-            for (int i = r0 + threadIdx.x + kCgRegRows * kCgThreads; i < r1; i += kCgThreads) {
-                const DF3 d = ld_row(V.d2, i), r = ld_row(V.r2, i);
-                DF3 z;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) z.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
-                direction(i, z, ld_row(V.p2, i));
+                for (int c = 0; c < 3; ++c) {
+                    p.v[c] = df_madd(beta, p.v[c], u.v[c]);
+                    sr.v[c] = df_madd(beta, sr.v[c], wi.v[c]);
+                    x.v[c] = df_madd(alpha, p.v[c], x.v[c]);
+                    r.v[c] = df_madd(nalpha, sr.v[c], r.v[c]);
+                    un.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
+                }
+                st_row(pv, i, p);
+                st_row(sv, i, sr);
+                st_row(xv, i, x);
+                st_row(rv, i, r);
+                st_row(uv, i, un);
+                bad |= df3_out_of_range(r) || df3_out_of_range(p);
             }
-            if (__syncthreads_or(bad)) {
-                // Every block takes the same decision: the flag goes through the next sums.
-                if (threadIdx.x == 0) atomicExch(&S->status, kCgOutOfRange);
-            }
-            cg_grid_sync(S, gen);
-        }
-        if (cg_status(S) == kCgOutOfRange) {
-            out_of_range = true;
-            break;
+            cg_grid_sync(S, gen);  // u complete before the next product
         }
     }
     if (reporter) {
