@@ -1024,7 +1024,7 @@ struct ImplicitSolver {
                           &d_p, &d_Ap, &d_dinv})
             SPGX_TRY_STATUS(b->alloc(vb));
         for (DevBuf *b : {&d_x2, &d_r2, &d_p2, &d_Ap2, &d_d2, &d_u2, &d_w2})
-            SPGX_TRY_STATUS(b->alloc(size_t(std::max(1, nv)) * 2 * sizeof(float4)));
+            SPGX_TRY_STATUS(b->alloc(size_t(std::max(1, nv)) * 3 * sizeof(float2)));
         SPGX_TRY_STATUS(d_wide.alloc(sizeof(int)));
         SPGX_TRY_STATUS(d_sync.alloc(sizeof(CgSync)));
         SPGX_TRY_STATUS(h_sync.alloc(sizeof(CgSync)));
@@ -1134,8 +1134,8 @@ struct ImplicitSolver {
         implicit_split_kernel<<<kSplitBlocks, 256, 0, stream>>>(T, d_uval.as<float2>(), d_ufull.as<int>(), SD.nnzu, nv);
         SPGX_CUDA(cudaMemsetAsync(d_sync.as<void>(), 0, sizeof(CgSync), stream));
         SPGX_CUDA(cudaGetLastError());
-        CgDfVecs V{vec(d_b), vec(d_dinv), vec(d_dx), d_x2.as<float4>(), d_r2.as<float4>(), d_p2.as<float4>(),
-                   d_Ap2.as<float4>(), d_d2.as<float4>(), d_u2.as<float4>(), d_w2.as<float4>(), d_part.as<double>(), n,
+        CgDfVecs V{vec(d_b), vec(d_dinv), vec(d_dx), d_x2.as<float2>(), d_r2.as<float2>(), d_p2.as<float2>(),
+                   d_Ap2.as<float2>(), d_d2.as<float2>(), d_u2.as<float2>(), d_w2.as<float2>(), d_part.as<double>(), n,
                    nv};
         CgSync *sync = d_sync.as<CgSync>();
         CgControl *ctl = d_ctl.as<CgControl>();

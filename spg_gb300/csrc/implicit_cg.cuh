@@ -40,14 +40,14 @@ struct CgSymDf {
 };
 constexpr int kCgBlockFloat4 = 5;
 
-// The solve's vectors: one 32-byte record per row (vertex), {x.hi, x.lo, y.hi, y.lo} and
-// {z.hi, z.lo, 0, 0}, so that a gathered neighbour is one sector.
+// The solve's vectors: one 24-byte record per row (vertex), {x.hi, x.lo}, {y.hi, y.lo},
+// {z.hi, z.lo}: the vector pass streams twelve of them per row and iteration.
 struct CgDfVecs {
     const double *b;     // right-hand side (FP64, 3 per row)
     const double *dinv;  // diagonal preconditioner 1 / A_ii (FP64, 3 per row)
     double *x;           // the solution, written in FP64 at the end
-    float4 *x2, *r2, *p2, *Ap2, *d2;  // Ap2 holds s = A p (kept by recurrence)
-    float4 *u2, *w2;                   // u = D^-1 r and w = A u
+    float2 *x2, *r2, *p2, *Ap2, *d2;  // Ap2 holds s = A p (kept by recurrence)
+    float2 *u2, *w2;                   // u = D^-1 r and w = A u
     double *part;        // per barrier parity and block: {p.Ap, r.r, r.z, out of range}
     int n, nv;
 };
@@ -83,16 +83,17 @@ struct DF3 {
 // barrier's acquire and the CTA barrier that follows it, they see every block's writes, and the
 // neighbours a block gathers (rows a few hundred apart in reverse Cuthill-McKee order) mostly
 // hit its L1. The read-only path (__ldg) is kept for the matrix, which the launch never writes.
-__device__ __forceinline__ DF3 ld_row(const float4 *P, int i)
+__device__ __forceinline__ DF3 ld_row(const float2 *P, int i)
 {
-    const float4 a = P[2 * size_t(i)];
-    const float2 b = *reinterpret_cast<const float2 *>(P + 2 * size_t(i) + 1);
-    return {{make_float2(a.x, a.y), make_float2(a.z, a.w), b}};
+    const float2 *q = P + 3 * size_t(i);
+    return {{q[0], q[1], q[2]}};
 }
-__device__ __forceinline__ void st_row(float4 *P, int i, const DF3 &r)
+__device__ __forceinline__ void st_row(float2 *P, int i, const DF3 &r)
 {
-    P[2 * size_t(i)] = make_float4(r.v[0].x, r.v[0].y, r.v[1].x, r.v[1].y);
-    *reinterpret_cast<float2 *>(P + 2 * size_t(i) + 1) = r.v[2];
+    float2 *q = P + 3 * size_t(i);
+    q[0] = r.v[0];
+    q[1] = r.v[1];
+    q[2] = r.v[2];
 }
 __device__ __forceinline__ bool df3_out_of_range(const DF3 &r)
 {
@@ -337,9 +338,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
             const float2 alpha = split_df(alpha_d, o);
             const float2 nalpha = df_neg(alpha);
             bad = o || df_out_of_range(beta);
-            float4 *__restrict__ xv = V.x2, *__restrict__ rv = V.r2, *__restrict__ pv = V.p2,
+            float2 *__restrict__ xv = V.x2, *__restrict__ rv = V.r2, *__restrict__ pv = V.p2,
                                  *__restrict__ sv = V.Ap2, *__restrict__ uv = V.u2;
-            const float4 *__restrict__ wv = V.w2, *__restrict__ dv = V.d2;
+            const float2 *__restrict__ wv = V.w2, *__restrict__ dv = V.d2;
             for (int i = r0 + threadIdx.x; i < r1; i += kCgThreads) {
                 DF3 p = ld_row(pv, i), sr = ld_row(sv, i), x = ld_row(xv, i), r = ld_row(rv, i);
                 const DF3 u = ld_row(uv, i), wi = ld_row(wv, i), d = ld_row(dv, i);
