@@ -449,6 +449,11 @@ spgx_status spgx_implicit_reset(spgx_implicit *h);
 spgx_status spgx_implicit_set_params(spgx_implicit *h, const spgx_implicit_params *params);
 /* The robust methods' current substep (m_currentDt; -1 before the first step). */
 spgx_status spgx_implicit_get_step_size(spgx_implicit *h, double *dt);
+/* Failure-detection test hook: the next double-float CG solve starts its grid barrier counter
+ * where no barrier completes, so that its bounded waits run out (about a second). The step
+ * returns SPGX_ERR_TIMEOUT with the positions of that step incomplete; restore a saved state
+ * with spgx_implicit_set_state and step on. Nothing faults or hangs. */
+spgx_status spgx_implicit_test_stall(spgx_implicit *h);
 
 /* ------------------------------------------------------------------------------------ */
 /* XPBD (one projection sweep per substep, xpbd.h:13-15)                                  */

@@ -834,6 +834,7 @@ struct ImplicitSolver {
     HostBuf h_dots, h_ctl, h_sync;
     CgSymDf SD{};
     int cg_lanes{4}, cg_blocks{0};
+    bool stall_next{false};  // test hook: the next double-float solve's barrier waits run out
     std::vector<int32_t> row_of;  // the CG's row of each vertex (scene order over all objects)
     cudaGraphExec_t cg_graph{nullptr};
     ImplicitTables T{};
@@ -1133,6 +1134,10 @@ struct ImplicitSolver {
         SPGX_CUDA(cudaMemsetAsync(T.wide, 0, sizeof(int), stream));
         implicit_split_kernel<<<kSplitBlocks, 256, 0, stream>>>(T, d_uval.as<float2>(), d_ufull.as<int>(), SD.nnzu, nv);
         SPGX_CUDA(cudaMemsetAsync(d_sync.as<void>(), 0, sizeof(CgSync), stream));
+        if (stall_next) {  // test hook: a barrier counter no barrier completes from
+            SPGX_CUDA(cudaMemsetAsync(d_sync.as<void>(), 0x80, sizeof(int), stream));
+            stall_next = false;
+        }
         SPGX_CUDA(cudaGetLastError());
         CgDfVecs V{vec(d_b), vec(d_dinv), vec(d_dx), d_x2.as<float2>(), d_r2.as<float2>(), d_p2.as<float2>(),
                    d_Ap2.as<float2>(), d_d2.as<float2>(), d_u2.as<float2>(), d_w2.as<float2>(), d_part.as<double>(), n,
@@ -1637,6 +1642,15 @@ spgx_status spgx_implicit_get_step_size(spgx_implicit *h, double *dt)
         return SPGX_ERR_INVALID_ARG;
     }
     *dt = h->s->current_dt;
+    return SPGX_OK;
+    SPGX_GUARD_END
+}
+
+spgx_status spgx_implicit_test_stall(spgx_implicit *h)
+{
+    SPGX_GUARD_BEGIN
+    SPGX_IHANDLE(h);
+    h->s->stall_next = true;
     return SPGX_OK;
     SPGX_GUARD_END
 }

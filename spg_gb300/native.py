@@ -152,6 +152,7 @@ def lib():
         L.spgx_implicit_set_state.argtypes = [vp, i32, dp, dp]
         L.spgx_implicit_reset.argtypes = [vp]
         L.spgx_implicit_get_step_size.argtypes = [vp, dp]
+        L.spgx_implicit_test_stall.argtypes = [vp]
         L.spgx_implicit_set_params.argtypes = [vp, C.POINTER(ImplicitParams)]
         _lib = L
     return _lib
@@ -463,6 +464,10 @@ class ImplicitSolver:
         d = C.c_double()
         check(lib().spgx_implicit_get_step_size(self.h, C.byref(d)))
         return d.value
+
+    def test_stall(self):
+        """Failure-detection test hook: the next CG solve's bounded barrier waits run out."""
+        check(lib().spgx_implicit_test_stall(self.h))
 
 
 class XpbdSolver:

@@ -1,5 +1,6 @@
 """Failure detection without a GPU fault: a bounded device-side wait that runs out is
-reported as a status, and the solver keeps working (the dataflow kernel's tile waits)."""
+reported as a status, and the solver keeps working (the VBD dataflow kernel's tile waits,
+the XPBD persistent kernels' waits, the CG launch's grid barriers)."""
 import time
 
 import numpy as np
@@ -76,3 +77,30 @@ def test_xpbd_persistent_wait_runs_out_and_the_solver_recovers(kernel):
     twin.step()
     assert np.array_equal(s.state(0)[0], twin.state(0)[0])
     print(f"stalled XPBD step returned after {elapsed:.2f} s")
+
+
+def test_cg_barrier_wait_runs_out_and_the_solver_recovers():
+    """The implicit solvers' CG launch: a grid barrier counter that no barrier completes makes
+    every bounded wait run out; the step returns a timeout status, and restored to the state
+    before that step the handle steps like a twin that never stalled (to 1e-9 m: the FP64
+    assembly adds with atomics in no fixed order, and the CG amplifies those last-bit
+    differences to about 1e-12 m)."""
+    obj = scenes.truss_variant()
+    kw = dict(dt=1 / 60, substeps=1, gravity=scenes.GRAVITY)
+    s = N.ImplicitSolver([obj], **kw)
+    twin = N.ImplicitSolver([obj], **kw)
+    s.step()
+    twin.step()
+    x0, v0 = s.state(0)
+    s.test_stall()
+    t0 = time.time()
+    with pytest.raises(N.SpgxError) as err:
+        s.step()
+    elapsed = time.time() - t0
+    assert err.value.status == SPGX_ERR_TIMEOUT, err.value
+    assert elapsed < 30, elapsed
+    s.set_state(0, x0, v0)
+    s.step()
+    twin.step()
+    assert np.abs(s.state(0)[0] - twin.state(0)[0]).max() <= 1e-9
+    print(f"stalled CG step returned after {elapsed:.2f} s")
