@@ -1128,7 +1128,7 @@ struct ImplicitSolver {
     // cooperative launch; when the system leaves that range it runs again in FP64.
     spgx_status cg(double alpha, double beta, int &iterations, double &rel_residual)
     {
-        const int nv = L.nv, n = n3();
+        const int nv = L.nv;
         implicit_lhs_kernel<<<grid_of(nv), 256, 0, stream>>>(T, vec(d_mass), nv, alpha, beta, vec(d_dinv));
         if (P.cg_precision == 1) return cg_fp64(iterations, rel_residual);
         SPGX_CUDA(cudaMemsetAsync(T.wide, 0, sizeof(int), stream));
@@ -1140,8 +1140,7 @@ struct ImplicitSolver {
         }
         SPGX_CUDA(cudaGetLastError());
         CgDfVecs V{vec(d_b), vec(d_dinv), vec(d_dx), d_x2.as<float2>(), d_r2.as<float2>(), d_p2.as<float2>(),
-                   d_Ap2.as<float2>(), d_d2.as<float2>(), d_u2.as<float2>(), d_w2.as<float2>(), d_part.as<double>(), n,
-                   nv};
+                   d_Ap2.as<float2>(), d_d2.as<float2>(), d_u2.as<float2>(), d_w2.as<float2>(), d_part.as<double>(), nv};
         CgSync *sync = d_sync.as<CgSync>();
         CgControl *ctl = d_ctl.as<CgControl>();
         const int *wide = T.wide;

@@ -49,7 +49,7 @@ struct CgDfVecs {
     float2 *x2, *r2, *p2, *Ap2, *d2;  // Ap2 holds s = A p (kept by recurrence)
     float2 *u2, *w2;                   // u = D^-1 r and w = A u
     double *part;        // per barrier parity and block: {p.Ap, r.r, r.z, out of range}
-    int n, nv;
+    int nv;
 };
 
 struct CgSync {
