@@ -226,8 +226,10 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
     // grid reduction per iteration instead of two. The stopping test (|r|^2 < tol^2 |b|^2 after
     // an update, or max_its updates) and the iteration count are those of the FP64 path.
 
-    // Start (x = 0, p = s = 0): r = b, u = D^-1 r.
+    // Start (x = 0, p = s = 0): r = b, u = D^-1 r. r.u and r.r are summed where r and u are
+    // formed (here and in the vector pass) and reduced with the next product's u.w.
     bool bad = false;
+    float2 ru_part = make_float2(0.f, 0.f), rr_part = ru_part;
     {
         const DF3 zero3{{make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)}};
         for (int i = r0 + threadIdx.x; i < r1; i += kCgThreads) {
@@ -238,6 +240,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
                 r.v[c] = split_df(V.b[3 * size_t(i) + c], o1);
                 d.v[c] = split_df(V.dinv[3 * size_t(i) + c], o2);
                 u.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
+                ru_part = df_madd(r.v[c], u.v[c], ru_part);
+                rr_part = df_madd(r.v[c], r.v[c], rr_part);
                 bad |= o1 | o2;
             }
             st_row(V.x2, i, zero3);
@@ -255,9 +259,9 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
     bool out_of_range = false;
 
     for (int k = 0; !cg_status(S); ++k) {
-        // w = A u (upper blocks, then the transposes of the lower ones); r.u, r.r, u.w.
+        // w = A u (upper blocks, then the transposes of the lower ones); u.w.
         {
-            float2 ru = make_float2(0.f, 0.f), rr = ru, uw = ru;
+            float2 uw = make_float2(0.f, 0.f);
             const int w = threadIdx.x >> 5, lane = threadIdx.x & (LANES - 1);
             for (int base = r0 + w * (32 / LANES); base < r1; base += kCgThreads / LANES) {
                 const int i = base + (threadIdx.x & 31) / LANES;
@@ -289,17 +293,13 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
                 if (i < r1 && lane == 0) {
                     const DF3 wi{{df_norm(h[0], l[0]), df_norm(h[1], l[1]), df_norm(h[2], l[2])}};
                     st_row(V.w2, i, wi);
-                    const DF3 ri = ld_row(V.r2, i), ui = ld_row(V.u2, i);
+                    const DF3 ui = ld_row(V.u2, i);
 #pragma unroll
-                    for (int r = 0; r < 3; ++r) {
-                        ru = df_madd(ri.v[r], ui.v[r], ru);
-                        rr = df_madd(ri.v[r], ri.v[r], rr);
-                        uw = df_madd(ui.v[r], wi.v[r], uw);
-                    }
+                    for (int r = 0; r < 3; ++r) uw = df_madd(ui.v[r], wi.v[r], uw);
                     bad |= df3_out_of_range(wi);
                 }
             }
-            cg_allreduce(V, S, gen, ru, rr, uw, bad, s_tot);
+            cg_allreduce(V, S, gen, ru_part, rr_part, uw, bad, s_tot);
         }
         if (cg_status(S)) break;
         const double gamma = s_tot[0], rr = s_tot[1], delta = s_tot[2];
@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
             const float2 alpha = split_df(alpha_d, o);
             const float2 nalpha = df_neg(alpha);
             bad = o || df_out_of_range(beta);
+            ru_part = rr_part = make_float2(0.f, 0.f);
             float2 *__restrict__ xv = V.x2, *__restrict__ rv = V.r2, *__restrict__ pv = V.p2,
                                  *__restrict__ sv = V.Ap2, *__restrict__ uv = V.u2;
             const float2 *__restrict__ wv = V.w2, *__restrict__ dv = V.d2;
@@ -352,6 +353,8 @@ __global__ void __launch_bounds__(kCgThreads, 1) implicit_cg_df_kernel(CgSymDf A
                     x.v[c] = df_madd(alpha, p.v[c], x.v[c]);
                     r.v[c] = df_madd(nalpha, sr.v[c], r.v[c]);
                     un.v[c] = df_madd(d.v[c], r.v[c], make_float2(0.f, 0.f));
+                    ru_part = df_madd(r.v[c], un.v[c], ru_part);
+                    rr_part = df_madd(r.v[c], r.v[c], rr_part);
                 }
                 st_row(pv, i, p);
                 st_row(sv, i, sr);
