@@ -464,7 +464,7 @@ typedef struct spgx_xpbd_params {
     double dt;
     int32_t substeps;
     double gravity[3];
-    int32_t block_size; /* one launch per phase: threads per block, 0 = default */
+    int32_t block_size; /* one launch per phase: threads per block, 0 = default (32) */
     int32_t use_graph;  /* one launch per phase: replay the step as a CUDA graph */
     int32_t device;
     int32_t kernel;     /* 0 = default (1); 1 = one launch per (energy, stencil colour) phase;

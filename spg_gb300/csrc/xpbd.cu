@@ -611,7 +611,10 @@ struct XpbdSolver {
         SPGX_TRY_STATUS(check_params(params));
         P = *params;
         h_sub = P.dt / P.substeps;
-        block = P.block_size ? P.block_size : 128;
+        // One warp per block by default: a phase's few tens of thousands of stencils then spread
+        // over every SM (513^2 cloth: 3.48 ms per step, against 3.55, 3.64 and 3.76 ms with 64,
+        // 128 and 256 threads).
+        block = P.block_size ? P.block_size : 32;
         SPGX_TRY_STATUS(select_device(P.device));
         device = P.device;
         SPGX_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
