@@ -38,6 +38,65 @@ def test_oracle_cg_matches_direct_solve():
     assert np.allclose(x, spla.spsolve(A.tocsc(), b), rtol=1e-8, atol=1e-10)
 
 
+def _chronopoulos_gear_cg(A, b, tol=1e-5, max_iterations=300):
+    """The recurrences of the GPU solve (implicit_cg.cuh), restated in FP64: u = D^-1 r,
+    w = A u, gamma = r.u, delta = u.w, beta = gamma / gamma_prev,
+    alpha = gamma / (delta - beta gamma / alpha_prev), p = u + beta p, s = w + beta s,
+    x += alpha p, r -= alpha s; the stopping test after each update."""
+    n = b.shape[0]
+    x, p, s = np.zeros(n), np.zeros(n), np.zeros(n)
+    rhs2 = float(b @ b)
+    d = A.diagonal()
+    inv = np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 1.0)
+    thr = max(tol * tol * rhs2, np.finfo(float).tiny)
+    r = b.copy()
+    u = inv * r
+    its, gamma_prev, alpha_prev = 0, 0.0, 1.0
+    for k in range(max_iterations + 1):
+        w = A @ u
+        gamma, rr, delta = float(r @ u), float(r @ r), float(u @ w)
+        if k == 0:
+            if rhs2 == 0.0 or rr < thr:
+                break
+        else:
+            its += 1
+            if rr < thr or its >= max_iterations:
+                break
+        beta = 0.0 if k == 0 else gamma / gamma_prev
+        alpha = gamma / (delta - beta * gamma / alpha_prev)
+        p = u + beta * p
+        s = w + beta * s
+        x += alpha * p
+        r -= alpha * s
+        u = inv * r
+        gamma_prev, alpha_prev = gamma, alpha
+    return x, its, np.sqrt(rr / rhs2) if rhs2 else 0.0
+
+
+def test_chronopoulos_gear_recurrences_match_the_reference_cg():
+    """The GPU solve's form of preconditioned CG (one reduction per iteration) takes the same
+    iterates as Eigen's (the oracle's restatement): on random SPD systems with a spread of
+    diagonal scales (condition numbers near 4e4), the same iteration count, and solutions within
+    1e-10 relative when the solve converges."""
+    rng = np.random.default_rng(3)
+    for n, density in ((60, 0.1), (200, 0.03), (500, 0.01)):
+        B = sp.random(n, n, density=density, random_state=int(rng.integers(1 << 30)))
+        D = sp.diags(10.0 ** rng.uniform(-1, 1, size=n))
+        A = (D @ (B @ B.T + sp.eye(n) * 0.5) @ D).tocsr()
+        b = rng.normal(size=n)
+        for tol, cap in ((1e-8, 1000), (1e-5, 20)):
+            x_ref, it_ref, rel_ref = IR.conjugate_gradient(A, b, tol=tol, max_iterations=cap)
+            x_cg, it_cg, rel_cg = _chronopoulos_gear_cg(A, b, tol=tol, max_iterations=cap)
+            assert it_cg == it_ref, (n, tol, it_cg, it_ref)
+            err = np.abs(x_cg - x_ref).max() / np.abs(x_ref).max()
+            if it_ref < cap:  # converged: both residuals under the tolerance, the same x
+                assert rel_cg < tol and rel_ref < tol
+                assert err <= 1e-10, (n, tol, err)
+            else:  # stopped by the cap mid-solve, where rounding has grown (measured <= 4e-9)
+                assert err <= 1e-7, (n, tol, err)
+                assert abs(rel_cg - rel_ref) <= 1e-2 * rel_ref
+
+
 def test_oracle_steps_every_scene():
     for name, obj in _scenes().items():
         s = IR.ImplicitEuler(obj, 1 / 60, 1, scenes.GRAVITY)
