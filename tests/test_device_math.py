@@ -71,3 +71,24 @@ def test_reciprocal_within_one_ulp():
     print(f"reciprocal: max {e.max():.2f} ulp")
     assert e.max() <= 1.0
     assert np.isinf(_run(np.zeros(1), np.zeros(1))[2][0])
+
+
+def test_arctan2_coefficients_are_the_fit_scripts_output():
+    """The nine float32 literals of the device arctan2's polynomial (elements.cuh) are what
+    atan_poly_fit.py beside it produces (Remez exchange, degree 8), bit for bit, and that
+    polynomial's float32 Horner evaluation stays within 2 ulp of atan on [0, 1]."""
+    import importlib.util
+    import re
+    csrc = os.path.join(os.path.dirname(HERE), "spg_gb300", "csrc")
+    spec = importlib.util.spec_from_file_location("atan_poly_fit", os.path.join(csrc, "atan_poly_fit.py"))
+    fit = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fit)
+    c32 = fit.remez(fit.DEGREE).astype(np.float32)
+    src = open(os.path.join(csrc, "elements.cuh")).read()
+    body = src[src.index("SPGX_HD float arctan2(float y, float x)"):]
+    body = body[:body.index("float r = t * p;")]
+    lits = [float(v) for v in re.findall(r"p = (-?[0-9.e-]+)f;", body)]
+    lits += [float(v) for v in re.findall(r"p = fmaf\(p, s, (-?[0-9.e-]+)f\);", body)]
+    # highest degree first in the Horner chain; the script lists degree 0 first
+    assert np.array_equal(np.array(lits[::-1], np.float32), c32)
+    assert fit.float32_ulp_error(c32) <= 2.0
