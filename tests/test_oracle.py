@@ -141,7 +141,9 @@ def test_literal_colouring_matches_reference_golden(golden):
         del s
 
 
-def test_scene_counts_match_survey_table(golden):
+def test_scene_counts_of_the_benchmark_scenes(golden):
+    """Vertex, incidence, colour and stencil counts of the 33^2 StVK cloth, the 41x11x11 six-tet
+    bar and the 513^2 spring cloth, as the reference's scene builders give them."""
     g1, g2, g3 = golden["cloth_33"], golden["beam_41x11x11_6tet"], golden["spring_cloth_513"]
     assert (g1["n_vertices"], g1["n_incidences"], g1["n_colors"]) == (1089, 18178, 7)
     assert [e["n_stencils"] for e in g1["energies"]] == [3008, 2048, 2]
