@@ -1,6 +1,7 @@
-"""bench.py's roofline inputs on the CPU: the algorithmic bytes of the 513x513 spring cloth
-(one compulsory pass per iteration, 243 B per vertex-solve) and the DRAM traffic per sweep
-recorded from the committed ncu summaries of the VBD kernels."""
+"""bench.py's host-side pieces on the CPU: the algorithmic bytes of the 513x513 spring cloth
+(one compulsory pass per iteration, 243 B per vertex-solve; one XPBD substep), the DRAM
+traffic per sweep recorded from the committed ncu summaries of the VBD kernels, and the
+summary of the clocks sampled during the timed region."""
 import json
 import os
 
@@ -32,3 +33,31 @@ def test_recorded_traffic_is_near_the_algorithmic_bytes(kernel):
     t = bench._traffic_per_iteration(kernel)
     assert t == float(rec["dram_bytes_per_sweep"])
     assert 0.9 * 64012368 < t < 40 * 64012368
+
+
+def test_xpbd_algorithmic_bytes_of_the_513_cloth():
+    """One substep's compulsory bytes: 787,456 spring records x 20 B, 785,408 bending records
+    x 32 B, 513 anchor records x 28 B, and 132 B of vertex state per vertex."""
+    bench = pytest.importorskip("bench")
+    from spg_gb300 import scenes as S
+    obj = S.spring_cloth(513).objects[0]
+    expect = 20 * 787456 + 32 * 785408 + 28 * 513 + 132 * 263169
+    assert bench.xpbd_algorithmic_bytes_per_substep(obj) == expect == 75634848
+
+
+def test_clock_sampler_summary():
+    """The clocks record of the timed region: median SM clock, the highest max clock, and the
+    throttle reasons seen active in any sample; malformed and N/A lines are skipped."""
+    bench = pytest.importorskip("bench")
+    c = bench.ClockSampler(0)
+    c.lines = [
+        "2070, 2070, 910.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "1980, 2070, 1390.2, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "2055, 2070, 1200.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "[N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A], [N/A]",
+        "garbage",
+    ]
+    got = c.stop()
+    assert got == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    empty = bench.ClockSampler(0)
+    assert empty.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
