@@ -61,3 +61,12 @@ def test_clock_sampler_summary():
     assert got == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
     empty = bench.ClockSampler(0)
     assert empty.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def test_cpu_baseline_runs_whole_sweeps_of_the_oracle():
+    """The cpu_baseline leg: at least one whole colour sweep of the 513x513 cloth on every host
+    thread, reported as vertex-solves/s of the oracle ("port")."""
+    bench = pytest.importorskip("bench")
+    b = bench.cpu_baseline(0.1)
+    assert b["kind"] == "port" and b["unit"] == bench.UNIT and b["cores"] == (os.cpu_count() or 1)
+    assert b["value"] > 0 and "263169 vertex-solves" in b["sample"]
